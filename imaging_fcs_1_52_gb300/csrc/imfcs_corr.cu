@@ -1,0 +1,452 @@
+// imfcs_corr.cu -- streaming multi-tau correlator with blocked variance.
+//
+// Restates calculateCF (Imaging_FCS_1_52.java:9425-9648) for every output
+// pixel at once.  One CTA owns 32 output pixels (one per lane) and streams
+// the whole stack through shared memory in chunks of 128 frames:
+//
+//   stage   all warps compute the binned, background-subtracted,
+//           bleach-corrected and centred value of each (pixel, frame) and
+//           build the pairwise-binned levels 1..Q-1 (java:9467-9476),
+//   correlate
+//           warp 0: level 0, lags 0..8        warp 1: level 0, lags 9..16
+//           warp 2: levels 1..Q-1 (lag delays 9..16 at each level)
+//
+// Products are grouped by their *direct* sample y: when the delayed samples
+// y..y+16 are present, every lag's product d0[y]*d1[y+d] is accumulated.
+// So the blocks of the blocked variance (2^(ind-k) products, java:9502-9511)
+// end at the same y for every lag of a level, and the per-block sums of the
+// direct and delayed samples come from two shared running sums plus the
+// window "heads" (sum of the first d delayed samples of a block).  With the
+// window means a, b known from the monitor pass, the centred block mean is
+//   P_z = (A_z - b B_z - a D_z + L a b) / L
+// exactly the Java blocked product (prod after binct pairwise means).
+// Values are FP32 centred on the pixel's mean; block sums are exact-order FP32,
+// totals are float-float.
+#include <math.h>
+
+#include "imfcs_internal.cuh"
+
+namespace imfcs {
+
+constexpr int kCorrThreads = 96;
+constexpr int kStatN = 5;   // per-lag block statistics: Ahi, Alo, S1, S2, r
+
+struct CorrOut {
+    double *acf, *var, *sd;
+    double *nb_mean, *nb_cov;
+    float *bprod;        // GLS: [pix][chanum-1][pnum_max]
+    int pnum_stride;
+    float *stats;        // scratch [chanum][kStatN][npix]
+    int gls;
+};
+
+__device__ __forceinline__ float &stat_ref(float *stats, int npix, int lag, int s, int pix)
+{
+    return stats[((size_t)lag * kStatN + s) * npix + pix];
+}
+
+// Block end for the lags [lagbase, lagbase+nl) of one level (out of line:
+// it runs once per 2^(ind-k) direct samples).  acc: the lags' block sums of
+// products; head_sm: this level's heads (stride 32); wsm: delayed samples
+// y+1..y+16 in shared memory (stride 32); z: block number.
+__device__ __noinline__ void block_end(const Job &j, const CorrOut &o, const float4 *mon, int pix,
+                                       int lagbase, int del0, int nl, float *acc, float B0,
+                                       float B1, float *head_sm, const float *wsm, int z, int L,
+                                       int pnum)
+{
+    float nh[kP + 1];
+    nh[0] = 0.f;
+    for (int d = 1; d <= kP; d++) nh[d] = nh[d - 1] + wsm[(d - 1) * 32];
+    const float invL = 1.f / (float)L;
+    for (int l = 0; l < nl; l++) {
+        const int d = del0 + l, lag = lagbase + l;
+        const float4 m = mon[(size_t)pix * j.chanum + lag];
+        const float a = m.x, b = m.y;
+        float D = B1 - head_sm[d * 32] + nh[d];
+        float P = (acc[l] - b * B0 - a * D + (float)L * a * b) * invL;
+        float &ahi = stat_ref(o.stats, j.npix, lag, 0, pix);
+        float &alo = stat_ref(o.stats, j.npix, lag, 1, pix);
+        ff t = {ahi, alo};
+        ff_add(t, acc[l]);
+        ahi = t.hi;
+        alo = t.lo;
+        if (z < pnum) {
+            float &r = stat_ref(o.stats, j.npix, lag, 4, pix);
+            if (z == 0) r = P;
+            float dv = P - r;
+            stat_ref(o.stats, j.npix, lag, 2, pix) += dv;
+            stat_ref(o.stats, j.npix, lag, 3, pix) += dv * dv;
+            if (o.gls && lag >= 1) o.bprod[((size_t)pix * (j.chanum - 1) + (lag - 1)) * o.pnum_stride + z] = P;
+        }
+        acc[l] = 0.f;
+    }
+    for (int d = 0; d <= kP; d++) head_sm[d * 32] = nh[d];
+}
+
+// Heads of the first block: sums of the first d delayed samples.
+__device__ __noinline__ void block_head_init(float *head_sm, const float *wsm)
+{
+    float h = 0.f;
+    head_sm[0] = 0.f;
+    for (int d = 1; d <= kP; d++) { h += wsm[(d - 1) * 32]; head_sm[d * 32] = h; }
+}
+
+// Process the direct samples of one level held in shared memory.
+// buf0/buf1: level buffers (already offset by lane), [kHist + nnew] x 32;
+// position i holds sample s_begin - kHist + i.  Direct samples are
+// positions [0, nnew).
+template <int NL, int DEL0, bool RING>
+__device__ __forceinline__ void correlate_level(const Job &j, const CorrOut &o, const float4 *mon,
+                                                int pix, int lagbase, const float *buf0,
+                                                const float *buf1, int nnew, int s_begin, int numbin,
+                                                int L, int pnum, float *acc, float &B0, float &B1,
+                                                float *head_sm)
+{
+    const int ybeg = s_begin - kHist;
+    if (ybeg >= numbin || ybeg + nnew <= 0) return;
+    if (RING) {
+        // register ring of delayed samples: w[(i + d) & 31] = buf1[i + d]
+        float w[32];
+#pragma unroll
+        for (int d = 0; d < kP; d++) w[d] = buf1[d * 32];
+        for (int base = 0; base < nnew; base += 32) {
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) {
+                const int i = base + jj;
+                w[(jj + kP) & 31] = buf1[(i + kP) * 32];
+                const float x0 = buf0[i * 32];
+                const int y = ybeg + i;
+                if (y < 0 || y >= numbin) continue;
+                if (y == 0) block_head_init(head_sm, buf1 + i * 32);
+#pragma unroll
+                for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, w[(jj + DEL0 + l) & 31], acc[l]);
+                B0 += x0;
+                B1 += w[jj & 31];
+                if ((y & (L - 1)) == L - 1) {
+                    float tmp[NL];
+#pragma unroll
+                    for (int l = 0; l < NL; l++) tmp[l] = acc[l];
+                    block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i + 1) * 32,
+                              y / L, L, pnum);
+#pragma unroll
+                    for (int l = 0; l < NL; l++) acc[l] = 0.f;
+                    B0 = 0.f;
+                    B1 = 0.f;
+                }
+            }
+        }
+    } else {
+        for (int i = 0; i < nnew; i++) {
+            const int y = ybeg + i;
+            if (y < 0 || y >= numbin) continue;
+            const float x0 = buf0[i * 32];
+            if (y == 0) block_head_init(head_sm, buf1 + i * 32);
+#pragma unroll
+            for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, buf1[(i + DEL0 + l) * 32], acc[l]);
+            B0 += x0;
+            B1 += buf1[i * 32];
+            if ((y & (L - 1)) == L - 1) {
+                float tmp[NL];
+#pragma unroll
+                for (int l = 0; l < NL; l++) tmp[l] = acc[l];
+                block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i + 1) * 32,
+                          y / L, L, pnum);
+#pragma unroll
+                for (int l = 0; l < NL; l++) acc[l] = 0.f;
+                B0 = 0.f;
+                B1 = 0.f;
+            }
+        }
+    }
+}
+
+// Shared-memory layout: per level k a buffer of (kHist + kChunk/2^k) x 32
+// floats for the direct trace, and (CCF only) one for the delayed trace.
+__host__ __device__ inline int level_cap(int k) { return kHist + (kChunk >> k); }
+__host__ __device__ inline int level_off(int k)
+{
+    int o = 0;
+    for (int i = 0; i < k; i++) o += level_cap(i) * 32;
+    return o;
+}
+
+// Per-level persistent state of warp 2 (levels >= 1) in shared memory:
+// acc[8], B0, B1, head[17] per level and lane.  Level 0 keeps acc, B0, B1 in
+// registers of warps 0 and 1; each of those warps has its own head[17].
+constexpr int kLvlState = 8 + 2 + kP + 1;
+constexpr int kHead0 = 2 * (kP + 1);
+
+template <bool CCF>
+__global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo *li_g,
+                                                            const void *stack,
+                                                            const float *bparams,
+                                                            const float *basis,
+                                                            const float4 *mon, const int *blk_ind,
+                                                            CorrOut o)
+{
+    extern __shared__ float smem[];
+    const int nlev = j.q;                 // levels 0..q-1
+    const int buf_floats = level_off(nlev);
+    float *buf0 = smem;
+    float *buf1 = CCF ? smem + buf_floats : smem;
+    float *lvl_state = smem + (CCF ? 2 : 1) * buf_floats;   // [level][kLvlState][32]
+    float *head0_sm = lvl_state + nlev * kLvlState * 32;     // [warp 0/1][kP+1][32]
+    __shared__ float sh_basis[kChunk * (kMaxPoly + 1)];
+    __shared__ int sh_numbin[kMaxLevels];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int pix = blockIdx.x * 32 + lane;
+    const bool pvalid = pix < j.npix;
+    const int pixc = pvalid ? pix : 0;
+    if (tid < kMaxLevels) sh_numbin[tid] = tid < nlev ? li_g->numbin[tid] : 0;
+
+    // trace origins and bleach parameters of this lane's pixel
+    int xa, ya, xb, yb;
+    trace_origin(j, pixc, xa, ya);
+    const int trb = CCF ? j.npix + pixc : pixc;
+    trace_origin(j, trb, xb, yb);
+    float bpa[kBleachStride], bpb[kBleachStride];
+#pragma unroll
+    for (int i = 0; i < kBleachStride; i++) {
+        bpa[i] = __ldg(&bparams[(size_t)pixc * kBleachStride + i]);
+        bpb[i] = CCF ? __ldg(&bparams[(size_t)trb * kBleachStride + i]) : bpa[i];
+    }
+    const int ind = pvalid ? blk_ind[pixc] : (j.q - 1);
+    const int pnum = li_g->pnum_by_ind[ind];
+
+    // zero the block statistics of this lane's lags
+    if (pvalid) {
+        int lag_lo, lag_hi;
+        if (warp == 0) { lag_lo = 0; lag_hi = 9; }
+        else if (warp == 1) { lag_lo = 9; lag_hi = 17; }
+        else { lag_lo = 17; lag_hi = j.chanum; }
+        for (int lag = lag_lo; lag < lag_hi; lag++)
+            for (int s = 0; s < kStatN; s++) stat_ref(o.stats, j.npix, lag, s, pix) = 0.f;
+    }
+    // zero level state and history
+    for (int i = tid; i < nlev * kLvlState * 32; i += kCorrThreads) lvl_state[i] = 0.f;
+    for (int k = 0; k < nlev; k++)
+        for (int i = tid; i < kHist * 32; i += kCorrThreads) {
+            buf0[level_off(k) + i] = 0.f;
+            if (CCF) buf1[level_off(k) + i] = 0.f;
+        }
+
+    // per-lag monitors of this warp's level-0 lags
+    float acc0[9], B00 = 0.f, B10 = 0.f;
+#pragma unroll
+    for (int l = 0; l < 9; l++) acc0[l] = 0.f;
+    for (int i = tid; i < kHead0 * 32; i += kCorrThreads) head0_sm[i] = 0.f;
+    __syncthreads();
+
+    const int order1 = j.poly_order + 1;
+    const int numbin_last = li_g->numbin[nlev - 1];
+    // number of chunks: until the top level has processed all direct samples
+    const int top_n = kChunk >> (nlev - 1);
+    int nchunks = (numbin_last + kHist + top_n - 1) / top_n;
+    const int nchunk0 = (j.num + kChunk - 1) / kChunk;
+    if (nchunks < nchunk0 + 1) nchunks = nchunk0 + 1;
+
+    for (int c = 0; c < nchunks; c++) {
+        const int f0 = c * kChunk;
+        // ---- stage: basis table for the chunk (polynomial bleach) ----
+        if (j.bleach == IMFCS_BLEACH_POLYNOMIAL)
+            for (int i = tid; i < kChunk * order1; i += kCorrThreads) {
+                int f = f0 + i / order1;
+                sh_basis[i] = f < j.num ? __ldg(&basis[(size_t)f0 * order1 + i]) : 0.f;
+            }
+        __syncthreads();
+        // ---- stage: level 0 values ----
+        if (f0 < j.num) {
+            for (int fr = warp; fr < kChunk; fr += kCorrThreads / 32) {
+                const int f = f0 + fr;
+                float va = 0.f, vb = 0.f;
+                if (f < j.num && pvalid) {
+                    float t = (float)(j.frametime_d * (f + 1.5));
+                    const float *bs = sh_basis + fr * order1;
+                    va = window_value(j, stack, xa, ya, f);
+                    if (j.bleach != IMFCS_BLEACH_NONE && bpa[11] != 0.f)
+                        va = bleach_correct(va, bleach_f(bpa, j.bleach, j.poly_order, t, bs), bpa[9], bpa[10]);
+                    va -= bpa[12];
+                    if (CCF) {
+                        vb = window_value(j, stack, xb, yb, f);
+                        if (j.bleach != IMFCS_BLEACH_NONE && bpb[11] != 0.f)
+                            vb = bleach_correct(vb, bleach_f(bpb, j.bleach, j.poly_order, t, bs), bpb[9], bpb[10]);
+                        vb -= bpb[12];
+                    }
+                }
+                buf0[level_off(0) + (kHist + fr) * 32 + lane] = va;
+                if (CCF) buf1[level_off(0) + (kHist + fr) * 32 + lane] = vb;
+            }
+        } else {
+            for (int i = tid; i < kChunk * 32; i += kCorrThreads) {
+                buf0[level_off(0) + kHist * 32 + i] = 0.f;
+                if (CCF) buf1[level_off(0) + kHist * 32 + i] = 0.f;
+            }
+        }
+        __syncthreads();
+        // ---- stage: levels 1..q-1 by pairwise sums (java:9467-9476) ----
+        for (int k = 1; k < nlev; k++) {
+            const int nk = kChunk >> k;
+            const int sb = c * nk;
+            for (int i = tid; i < nk * 32; i += kCorrThreads) {
+                int s = i >> 5, ln = i & 31;
+                bool v = (sb + s) < sh_numbin[k];
+                const float *p0 = buf0 + level_off(k - 1) + (kHist + 2 * s) * 32 + ln;
+                buf0[level_off(k) + (kHist + s) * 32 + ln] = v ? p0[0] + p0[32] : 0.f;
+                if (CCF) {
+                    const float *p1 = buf1 + level_off(k - 1) + (kHist + 2 * s) * 32 + ln;
+                    buf1[level_off(k) + (kHist + s) * 32 + ln] = v ? p1[0] + p1[32] : 0.f;
+                }
+            }
+            __syncthreads();
+        }
+        // level-0 samples beyond numbin are already zero (frames >= num staged as 0)
+        // ---- correlate ----
+        if (pvalid) {
+            if (warp < 2) {
+                const int numbin0 = li_g->numbin[0];
+                const int L = 1 << ind;
+                float *hs = head0_sm + warp * (kP + 1) * 32 + lane;
+                if (warp == 0)
+                    correlate_level<9, 0, true>(j, o, mon, pix, 0, buf0 + level_off(0) + lane,
+                                                buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
+                                                pnum, acc0, B00, B10, hs);
+                else
+                    correlate_level<8, 9, true>(j, o, mon, pix, 9, buf0 + level_off(0) + lane,
+                                                buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
+                                                pnum, acc0, B00, B10, hs);
+            } else {
+                for (int k = 1; k < nlev; k++) {
+                    const int nk = kChunk >> k;
+                    const int numbin = li_g->numbin[k];
+                    const int sb = c * nk;
+                    if (sb - kHist >= numbin) continue;
+                    float *st = lvl_state + (size_t)k * kLvlState * 32;
+                    float acc[8], B0, B1;
+#pragma unroll
+                    for (int l = 0; l < 8; l++) acc[l] = st[l * 32 + lane];
+                    B0 = st[8 * 32 + lane];
+                    B1 = st[9 * 32 + lane];
+                    float *hs = st + 10 * 32 + lane;
+                    const int L = 1 << (ind - k);
+                    const int lagbase = (kP + 1) + (k - 1) * 8;
+                    if (nk >= 32)
+                        correlate_level<8, 9, true>(j, o, mon, pix, lagbase, buf0 + level_off(k) + lane,
+                                                    buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
+                                                    B0, B1, hs);
+                    else
+                        correlate_level<8, 9, false>(j, o, mon, pix, lagbase, buf0 + level_off(k) + lane,
+                                                     buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
+                                                     B0, B1, hs);
+#pragma unroll
+                    for (int l = 0; l < 8; l++) st[l * 32 + lane] = acc[l];
+                    st[8 * 32 + lane] = B0;
+                    st[9 * 32 + lane] = B1;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- shift history: last kHist samples of each level to the front ----
+        // (source and destination overlap for levels with fewer than kHist
+        // new samples, so read everything first, then write)
+        constexpr int kPer = (kHist * 32 + kCorrThreads - 1) / kCorrThreads;
+        for (int k = 0; k < nlev; k++) {
+            const int nk = kChunk >> k;
+            float v0[kPer], v1[kPer];
+#pragma unroll
+            for (int r = 0; r < kPer; r++) {
+                int i = tid + r * kCorrThreads;
+                v0[r] = i < kHist * 32 ? buf0[level_off(k) + nk * 32 + i] : 0.f;
+                v1[r] = (CCF && i < kHist * 32) ? buf1[level_off(k) + nk * 32 + i] : 0.f;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kPer; r++) {
+                int i = tid + r * kCorrThreads;
+                if (i < kHist * 32) {
+                    buf0[level_off(k) + i] = v0[r];
+                    if (CCF) buf1[level_off(k) + i] = v1[r];
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- finalise: remaining partial block into the totals, outputs ----
+    if (!pvalid) return;
+    int lag_lo, lag_hi;
+    if (warp == 0) lag_lo = 0, lag_hi = 9;
+    else if (warp == 1) lag_lo = 9, lag_hi = 17;
+    else lag_lo = 17, lag_hi = j.chanum;
+    for (int lag = lag_lo; lag < lag_hi; lag++) {
+        float rem;
+        if (warp < 2) {
+            rem = 0.f;
+#pragma unroll
+            for (int l = 0; l < 9; l++)
+                if (l == lag - lag_lo) rem = acc0[l];
+        } else {
+            int k = 1 + (lag - 17) / 8, l = (lag - 17) % 8;
+            rem = lvl_state[(size_t)k * kLvlState * 32 + l * 32 + lane];
+        }
+        float &ahi = stat_ref(o.stats, j.npix, lag, 0, pix);
+        float &alo = stat_ref(o.stats, j.npix, lag, 1, pix);
+        ff t = {ahi, alo};
+        ff_add(t, rem);
+        const double A = ff_val(t);
+        const double S1 = stat_ref(o.stats, j.npix, lag, 2, pix);
+        const double S2 = stat_ref(o.stats, j.npix, lag, 3, pix);
+        const float4 m = mon[(size_t)pix * j.chanum + lag];
+        const double n = li_g->prodnum[lag];
+        const double dmDm = (double)m.z * (double)m.w;
+        const double sumprod = A - n * (double)m.x * (double)m.y;
+        const double corav = sumprod / (n * dmDm);
+        const double pn = pnum;
+        const double bv = (S2 / pn - (S1 / pn) * (S1 / pn)) / ((pn - 1) * dmDm * dmDm);
+        double acf = corav;
+        if (o.gls) {
+            const double r = stat_ref(o.stats, j.npix, lag, 4, pix);
+            acf = (lag == 0) ? 0.0 : (S1 + pn * r) / (pn * dmDm);   // mcov (java:9526-9531)
+        }
+        if (o.acf) o.acf[(size_t)pix * j.chanum + lag] = acf;
+        if (o.var) o.var[(size_t)pix * j.chanum + lag] = bv;
+        if (o.sd) o.sd[(size_t)pix * j.chanum + lag] = sqrt(bv);
+        if (lag == 1) {
+            if (o.nb_mean) o.nb_mean[pix] = m.z;
+            if (o.nb_cov) o.nb_cov[pix] = sumprod / n;
+        }
+    }
+}
+
+template __global__ void corr_kernel<false>(Job, const LagInfo *, const void *, const float *,
+                                            const float *, const float4 *, const int *, CorrOut);
+template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, const float *,
+                                           const float *, const float4 *, const int *, CorrOut);
+
+// Host-visible launch helper.
+size_t corr_smem_bytes(int q, bool ccf)
+{
+    return (size_t)((ccf ? 2 : 1) * level_off(q) + q * kLvlState * 32 + kHead0 * 32) * sizeof(float);
+}
+
+cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
+                        const float *basis, const float4 *mon, const int *blk_ind, double *acf,
+                        double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
+                        int pnum_stride, float *stats, int gls, cudaStream_t stream)
+{
+    CorrOut o;
+    o.acf = acf; o.var = var; o.sd = sd; o.nb_mean = nb_mean; o.nb_cov = nb_cov;
+    o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls;
+    size_t smem = corr_smem_bytes(j.q, j.is_ccf);
+    dim3 grid((j.npix + 31) / 32);
+    if (j.is_ccf) {
+        cudaFuncSetAttribute(corr_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        corr_kernel<true><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o);
+    } else {
+        cudaFuncSetAttribute(corr_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        corr_kernel<false><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace imfcs

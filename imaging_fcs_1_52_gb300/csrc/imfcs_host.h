@@ -1,0 +1,65 @@
+// imfcs_host.h -- host-side declarations shared by the C-ABI translation units.
+#pragma once
+
+#include <string>
+
+#include "imfcs_internal.cuh"
+#include "imfcs_gb300.h"
+
+namespace imfcs {
+
+// launchers (defined in the kernel translation units)
+cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
+                        const float *basis, const float4 *mon, const int *blk_ind, double *acf,
+                        double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
+                        int pnum_stride, float *stats, int gls, cudaStream_t stream);
+size_t corr_smem_bytes(int q, bool ccf);
+
+struct FitArgs;
+cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream);
+struct EpilogueArgs;
+cudaError_t launch_fit_epilogue(const EpilogueArgs &e, cudaStream_t stream);
+cudaError_t launch_ols_prepare(int npix, int chanum, int fitstart, int npts, const double *acf,
+                               const double *var, float *y, float *w, cudaStream_t stream);
+cudaError_t launch_bayes_combine(int npix, const double *lp1, const double *lp2, float *prob,
+                                 cudaStream_t stream);
+struct GlsArgs;
+cudaError_t launch_gls(const GlsArgs &g, cudaStream_t stream);
+
+// prep launchers (imfcs_prep_launch.cu)
+cudaError_t launch_trace(const Job &j, const void *stack, float *trace, cudaStream_t s);
+cudaError_t launch_bleach(const Job &j, const float *trace, const double *proj, float uscale,
+                          float uoff, float *bparams, cudaStream_t s);
+cudaError_t launch_center_given(const Job &j, const float *trace, float *bparams, cudaStream_t s);
+cudaError_t launch_monitor(const Job &j, const LagInfo *li_dev, const void *stack,
+                           const float *bparams, const float *basis, const int *snap_pos, int nseg,
+                           float2 *segtot, float2 *snap_part, float4 *mon, float4 *blkmon,
+                           cudaStream_t s);
+cudaError_t launch_block(const Job &j, const void *stack, const float *bparams, const float *basis,
+                         const float4 *blkmon, int nbseg, float *s1, float *s2, float *segsum,
+                         int *ind, int *ok, cudaStream_t s);
+cudaError_t launch_binning(const float *in, float *out, int win, int hin, int wt, int ht,
+                           int frames, int bx, int by, cudaStream_t s);
+cudaError_t launch_bleach_average(const float *in, float *out, int w, int h, int nopit, int ave,
+                                  cudaStream_t s);
+
+// error state
+void set_error(const std::string &msg);
+std::string cuda_msg(cudaError_t e, const char *what);
+
+// Lag-table and structure set-up shared by the plan and the reference calcACF.
+bool build_lag_info(int p, int q, int num, LagInfo &li, int &chanum, int &blocknum,
+                    std::string &err);
+
+// Legendre projection for the polynomial bleach fit: proj[(order+1)][nopit]
+// (FP64, host), and the u-mapping of time.
+void legendre_projection(int order, int nopit, int ave, double frametime, double *proj,
+                         double &uscale, double &uoff);
+void legendre_basis_table(int order, int num, double frametime, double uscale, double uoff,
+                          float *table);
+
+int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h, bool given_bleach,
+                   imfcs_plan **plan_out);
+int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *dev_out, void *stream);
+
+}  // namespace imfcs

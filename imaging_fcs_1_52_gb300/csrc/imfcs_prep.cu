@@ -1,0 +1,700 @@
+// imfcs_prep.cu -- the passes in front of the correlator:
+//   trace_kernel       averaged intensity trace (calcIntensityTrace, java:9822-9855)
+//   bleach_*_kernel    polynomial / exponential bleach fits (java:10845-11004)
+//   monitor_kernel     prefix sums of the corrected, centred trace at the
+//                      window edges every lag's monitors need (java:9484-9491)
+//   block_kernel       lag-1 blocking curve of blockTransform (java:9217-9422)
+// All streaming passes read the stack once and are HBM-bound; they split the
+// time axis into segments so that every SM has enough loads in flight.
+#include <math.h>
+
+#include "imfcs_internal.cuh"
+#include "imfcs_host.h"
+
+namespace imfcs {
+
+// ---------------------------------------------------------------------------
+// Averaged trace: out[trace][x] = (int) sum_{ave frames, window} / ave.
+// Block (32 traces) x (8 rows); each thread computes 4 points; a shared tile
+// transposes the result so both reads and writes are coalesced.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) trace_kernel(Job j, const void *stack, float *trace_out)
+{
+    __shared__ float tile[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int trace = blockIdx.x * 32 + tx;
+    const int xbase = blockIdx.y * 32;
+    int x0 = 0, y0 = 0;
+    const bool valid = trace < j.ntrace;
+    if (valid) trace_origin(j, trace, x0, y0);
+    for (int r = 0; r < 4; r++) {
+        int xl = ty * 4 + r, x = xbase + xl;
+        float val = 0.f;
+        if (valid && x < j.nopit) {
+            int sum = 0;
+            for (int f = x * j.ave; f < (x + 1) * j.ave; f++) sum += window_value_int(j, stack, x0, y0, f);
+            val = (float)(sum / j.ave);
+        }
+        tile[tx][xl] = val;
+    }
+    __syncthreads();
+    for (int r = 0; r < 4; r++) {
+        int tl = ty * 4 + r, tr = blockIdx.x * 32 + tl, x = xbase + tx;
+        if (tr < j.ntrace && x < j.nopit) trace_out[(size_t)tr * j.nopit + x] = tile[tl][tx];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Polynomial bleach fit: least squares in the Legendre basis of
+// u = t * uscale + uoff (t = averaged-trace time), coefficients = proj * y
+// with the FP64 projection matrix proj[(order+1)][nopit] built on the host.
+// One warp per trace.  Also writes f0 = f(0), the centre c and flags.
+// ---------------------------------------------------------------------------
+__global__ void bleach_poly_kernel(Job j, const float *trace, const double *proj, float uscale,
+                                   float uoff, float *bp_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tr >= j.ntrace) return;
+    const int k = j.poly_order + 1;
+    const float *y = trace + (size_t)tr * j.nopit;
+    double c[kMaxPoly + 1];
+    for (int i = 0; i < k; i++) c[i] = 0.0;
+    for (int x = lane; x < j.nopit; x += 32) {
+        double yx = (double)__ldg(&y[x]);
+        for (int i = 0; i < k; i++) c[i] = fma(__ldg(&proj[(size_t)i * j.nopit + x]), yx, c[i]);
+    }
+    for (int i = 0; i < k; i++) c[i] = warp_sum_d(c[i]);
+    float cf[kMaxPoly + 1], lb[kMaxPoly + 1];
+    for (int i = 0; i < k; i++) cf[i] = (float)c[i];
+    legendre(uoff, j.poly_order, lb);    // u(0) = uoff
+    double f0 = 0.0;
+    for (int i = 0; i < k; i++) f0 += c[i] * (double)lb[i];
+    float f0f = (float)f0, inv_f0 = (float)(1.0 / f0);
+    // centre: mean of the corrected averaged trace
+    float csum = 0.f;
+    for (int x = lane; x < j.nopit; x += 32) {
+        float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
+        legendre(t * uscale + uoff, j.poly_order, lb);
+        float f = 0.f;
+        for (int i = 0; i < k; i++) f = fmaf(cf[i], lb[i], f);
+        csum += bleach_correct(__ldg(&y[x]), f, f0f, inv_f0);
+    }
+    csum = warp_sum(csum);
+    if (lane == 0) {
+        float *bp = bp_out + (size_t)tr * kBleachStride;
+        for (int i = 0; i < k; i++) bp[i] = cf[i];
+        bp[9] = f0f;
+        bp[10] = inv_f0;
+        bp[11] = (isfinite(f0) && f0 != 0.0) ? 1.f : 0.f;
+        bp[12] = csum / j.nopit;
+        bp[13] = uscale;
+        bp[14] = uoff;
+    }
+}
+
+// Centre only (no bleach correction): mean of the averaged trace.
+__global__ void center_kernel(Job j, const float *trace, float *bp_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tr >= j.ntrace) return;
+    const float *y = trace + (size_t)tr * j.nopit;
+    float s = 0.f;
+    for (int x = lane; x < j.nopit; x += 32) s += __ldg(&y[x]);
+    s = warp_sum(s);
+    if (lane == 0) {
+        float *bp = bp_out + (size_t)tr * kBleachStride;
+        bp[11] = 0.f;
+        bp[12] = s / j.nopit;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exponential bleach fits (SingleExp / DoubleExp, java:13028-13085) by an
+// FP32 Levenberg-Marquardt per warp, in scaled variables (t / tmax, y / ymax),
+// from the Java initial guesses (java:10862-10864, 10917-10921).
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void exp_eval(const float *p, float t, float &f, float *g)
+{
+    if (K == 3) {
+        float e = __expf(-t / p[1]);
+        f = p[0] * e + p[2];
+        g[0] = e;
+        g[1] = p[0] * t * e / (p[1] * p[1]);
+        g[2] = 1.f;
+    } else {
+        float e1 = __expf(-t / p[1]), e2 = __expf(-t / p[3]);
+        f = p[0] * e1 + p[2] * e2 + p[4];
+        g[0] = e1;
+        g[1] = p[0] * t * e1 / (p[1] * p[1]);
+        g[2] = e2;
+        g[3] = p[2] * t * e2 / (p[3] * p[3]);
+        g[4] = 1.f;
+    }
+}
+
+template <int K>
+__device__ bool solve_spd(float *a, const float *b, float *x)
+{
+    // in-place Cholesky (lower) of a (K x K) then solve
+    for (int c = 0; c < K; c++) {
+        float d = a[c * K + c];
+        for (int m = 0; m < c; m++) d -= a[c * K + m] * a[c * K + m];
+        if (!(d > 0.f)) return false;
+        d = sqrtf(d);
+        a[c * K + c] = d;
+        for (int r = c + 1; r < K; r++) {
+            float s = a[r * K + c];
+            for (int m = 0; m < c; m++) s -= a[r * K + m] * a[c * K + m];
+            a[r * K + c] = s / d;
+        }
+    }
+    float yv[K];
+    for (int r = 0; r < K; r++) {
+        float s = b[r];
+        for (int m = 0; m < r; m++) s -= a[r * K + m] * yv[m];
+        yv[r] = s / a[r * K + r];
+    }
+    for (int r = K - 1; r >= 0; r--) {
+        float s = yv[r];
+        for (int m = r + 1; m < K; m++) s -= a[m * K + r] * x[m];
+        x[r] = s / a[r * K + r];
+    }
+    return true;
+}
+
+template <int K>
+__global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tr >= j.ntrace) return;
+    const int n = j.nopit;
+    const float *y = trace + (size_t)tr * n;
+    const float tmax = (float)(j.frametime_d * (n - 0.5) * j.ave);
+    // scale of y
+    float ym = 0.f;
+    for (int x = lane; x < n; x += 32) ym = fmaxf(ym, fabsf(__ldg(&y[x])));
+    for (int o = 16; o > 0; o >>= 1) ym = fmaxf(ym, __shfl_xor_sync(0xffffffffu, ym, o));
+    if (ym == 0.f) ym = 1.f;
+    const float iy = 1.f / ym, it = 1.f / tmax;
+    float p[K];
+    {
+        float y1 = __ldg(&y[1]) * iy;
+        float thalf = (float)(j.frametime_d * (n / 2 + 0.5) * j.ave) * it;
+        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.f; }
+        else {
+            float t10 = (float)(j.frametime_d * (n / 10 + 0.5) * j.ave) * it;
+            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.f;
+        }
+    }
+    float lambda = 1e-3f, chi2 = 0.f;
+    float A[K * K], g[K];
+    bool ok = true;
+    auto accumulate = [&](const float *pp, float *AA, float *gg) -> float {
+        float c2 = 0.f;
+        float acc[K * (K + 1) / 2 + K + 1];
+        for (int i = 0; i < K * (K + 1) / 2 + K + 1; i++) acc[i] = 0.f;
+        for (int x = lane; x < n; x += 32) {
+            float t = (float)(j.frametime_d * (x + 0.5) * j.ave) * it;
+            float f, gr[K];
+            exp_eval<K>(pp, t, f, gr);
+            float r = __ldg(&y[x]) * iy - f;
+            int q = 0;
+            for (int a = 0; a < K; a++)
+                for (int b = 0; b <= a; b++) acc[q++] += gr[a] * gr[b];
+            for (int a = 0; a < K; a++) acc[q++] += gr[a] * r;
+            acc[q] += r * r;
+        }
+        for (int i = 0; i < K * (K + 1) / 2 + K + 1; i++) acc[i] = warp_sum(acc[i]);
+        int q = 0;
+        if (AA) {
+            for (int a = 0; a < K; a++)
+                for (int b = 0; b <= a; b++) { AA[a * K + b] = acc[q]; AA[b * K + a] = acc[q]; q++; }
+            for (int a = 0; a < K; a++) gg[a] = acc[q++];
+        } else q += K * (K + 1) / 2 + K;
+        c2 = acc[q];
+        return c2;
+    };
+    chi2 = accumulate(p, A, g);
+    if (!isfinite(chi2)) ok = false;
+    int it_n = 0;
+    for (it_n = 0; ok && it_n < 500; it_n++) {
+        float M[K * K], h[K], pn[K];
+        for (int a = 0; a < K * K; a++) M[a] = A[a];
+        for (int a = 0; a < K; a++) M[a * K + a] *= (1.f + lambda);
+        if (!solve_spd<K>(M, g, h)) { lambda *= 10.f; if (lambda > 1e20f) break; continue; }
+        float rel = 0.f;
+        for (int a = 0; a < K; a++) {
+            pn[a] = p[a] + h[a];
+            rel = fmaxf(rel, fabsf(h[a]) / fmaxf(fabsf(p[a]), 1e-6f));
+        }
+        float An[K * K], gn[K];
+        float c2n = accumulate(pn, An, gn);
+        if (isfinite(c2n) && c2n <= chi2) {
+            float dec = (chi2 - c2n) / fmaxf(chi2, 1e-30f);
+            for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
+            for (int a = 0; a < K * K; a++) A[a] = An[a];
+            chi2 = c2n;
+            lambda = fmaxf(lambda * 0.1f, 1e-7f);
+            if (dec < 1e-7f && rel < 1e-5f) break;
+        } else {
+            lambda *= 10.f;
+            if (lambda > 1e12f) break;
+        }
+    }
+    // back to data units
+    float res[5];
+    if (K == 3) { res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; }
+    else {
+        res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; res[3] = p[3] * tmax;
+        res[4] = p[4] * ym;
+    }
+    bool valid = ok;
+    for (int a = 0; a < K; a++) valid = valid && isfinite(res[a]);
+    // java:9689 / 9714: correction applied only when the product is nonzero
+    if (K == 3) valid = valid && (res[0] * res[1] != 0.f);
+    else valid = valid && (res[0] * res[1] * res[2] * res[3] != 0.f);
+    float f0 = (K == 3) ? res[0] + res[2] : res[0] + res[2] + res[4];
+    float inv_f0 = 1.f / f0;
+    float csum = 0.f;
+    for (int x = lane; x < n; x += 32) {
+        float yx = __ldg(&y[x]);
+        if (valid) {
+            float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
+            float f = (K == 3) ? res[0] * __expf(-t / res[1]) + res[2]
+                               : res[0] * __expf(-t / res[1]) + res[2] * __expf(-t / res[3]) + res[4];
+            yx = bleach_correct(yx, f, f0, inv_f0);
+        }
+        csum += yx;
+    }
+    csum = warp_sum(csum);
+    if (lane == 0) {
+        float *bp = bp_out + (size_t)tr * kBleachStride;
+        for (int a = 0; a < K; a++) bp[a] = res[a];
+        bp[9] = f0;
+        bp[10] = inv_f0;
+        bp[11] = valid ? 1.f : 0.f;
+        bp[12] = csum / n;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Corrected, centred frame value of a trace (the value the correlator uses).
+// basis: Legendre table [num][order+1] for the polynomial mode.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float corrected_delta(const Job &j, const void *stack, int x0, int y0,
+                                                 int t, const float *bp, const float *basis)
+{
+    float v = window_value(j, stack, x0, y0, t);
+    if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
+        float tt = (float)(j.frametime_d * (t + 1.5));
+        float f = bleach_f(bp, j.bleach, j.poly_order, tt,
+                           basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
+        v = bleach_correct(v, f, bp[9], bp[10]);
+    }
+    return v - bp[12];
+}
+
+// ---------------------------------------------------------------------------
+// Monitor pass: per (trace, segment of kSeg frames) the float-float segment
+// total of the centred trace and, for every snapshot position p inside the
+// segment, the partial sum from the segment start up to frame p-1.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) monitor_kernel(Job j, const void *stack,
+                                                      const float *bparams, const float *basis,
+                                                      const int *snap_pos, int nseg,
+                                                      float2 *segtot, float2 *snap_part)
+{
+    const int tr = blockIdx.x * blockDim.x + threadIdx.x;
+    const int seg = blockIdx.y;
+    if (tr >= j.ntrace) return;
+    int x0, y0;
+    trace_origin(j, tr, x0, y0);
+    const float *bp = bparams + (size_t)tr * kBleachStride;
+    float bpl[kBleachStride];
+    for (int i = 0; i < kBleachStride; i++) bpl[i] = __ldg(&bp[i]);
+    const int t0 = seg * kSeg, t1 = min(t0 + kSeg, j.num);
+    // first snapshot with position > t0
+    int lo = 0, hi = j.nsnap;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(&snap_pos[mid]) <= t0) lo = mid + 1; else hi = mid;
+    }
+    int sj = lo;
+    int next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
+    ff acc = {0.f, 0.f};
+    for (int t = t0; t < t1; t++) {
+        float d = corrected_delta(j, stack, x0, y0, t, bpl, basis);
+        ff_add(acc, d);
+        while (t + 1 == next) {
+            snap_part[(size_t)tr * j.nsnap + sj] = make_float2(acc.hi, acc.lo);
+            sj++;
+            next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
+        }
+    }
+    segtot[(size_t)tr * nseg + seg] = make_float2(acc.hi, acc.lo);
+}
+
+// Finalise monitors: one warp per output pixel.  Exclusive scan of the
+// segment totals (FP64), snapshot prefixes, then for every lag
+//   a = sum(direct window)/n - 2^k c0,  b = sum(delayed window)/n - 2^k c1,
+// dm = a + 2^k c0, Dm = b + 2^k c1  (java:9484-9491), plus the lag-1 monitors
+// of the zero-led sequence blockTransform reads (java:9259-9272).
+__global__ void monitor_finalize_kernel(Job j, const LagInfo *li, const float *bparams,
+                                        int nseg, const float2 *segtot, const float2 *snap_part,
+                                        float4 *mon, float4 *blkmon)
+{
+    extern __shared__ double sh[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int pix = blockIdx.x * (blockDim.x >> 5) + wid;
+    if (pix >= j.npix) return;
+    double *scan = sh + (size_t)wid * (nseg + 1 + 2 * j.nsnap);
+    double *pre0 = scan + nseg + 1;
+    double *pre1 = pre0 + j.nsnap;
+    for (int which = 0; which < (j.is_ccf ? 2 : 1); which++) {
+        int tr = which ? j.npix + pix : pix;
+        double *pre = which ? pre1 : pre0;
+        // exclusive scan of segment totals
+        double carry = 0.0;
+        for (int s0 = 0; s0 < nseg; s0 += 32) {
+            int s = s0 + lane;
+            double v = 0.0;
+            if (s < nseg) { float2 t = segtot[(size_t)tr * nseg + s]; v = (double)t.x + (double)t.y; }
+            double incl = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                double u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            if (s < nseg) scan[s] = carry + incl - v;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) scan[nseg] = carry;
+        __syncwarp();
+        for (int sj = lane; sj < j.nsnap; sj += 32) {
+            int p = li->snap_pos[sj];
+            double v = 0.0;
+            if (p > 0) {
+                int seg = (p - 1) / kSeg;
+                float2 t = snap_part[(size_t)tr * j.nsnap + sj];
+                v = scan[seg] + (double)t.x + (double)t.y;
+            }
+            pre[sj] = v;
+        }
+        __syncwarp();
+    }
+    if (!j.is_ccf)
+        for (int sj = lane; sj < j.nsnap; sj += 32) pre1[sj] = pre0[sj];
+    __syncwarp();
+    const double c0 = bparams[(size_t)pix * kBleachStride + 12];
+    const double c1 = bparams[(size_t)(j.is_ccf ? j.npix + pix : pix) * kBleachStride + 12];
+    for (int x = lane; x < j.chanum; x += 32) {
+        int k = li->level[x];
+        double n = li->prodnum[x];
+        double a = pre0[li->snap_dir_end[x]] / n;
+        double b = (pre1[li->snap_del_end[x]] - pre1[li->snap_del_beg[x]]) / n;
+        double sc = (double)(1 << k);
+        mon[(size_t)pix * j.chanum + x] =
+            make_float4((float)a, (float)b, (float)(a + sc * c0), (float)(b + sc * c1));
+    }
+    if (lane == 0) {
+        double T1 = j.num - 1;
+        double dm1 = (pre0[li->snap_tm2] + (j.num - 2) * c0) / T1;   // zero-led direct window
+        double Dm1 = (pre1[li->snap_tm1] + (j.num - 1) * c1) / T1;
+        blkmon[pix] = make_float4((float)(dm1 - c0), (float)(Dm1 - c1), (float)dm1, (float)Dm1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Blocking pass (blockTransform, java:9217-9422).  The lag-1 products of the
+// zero-led sequence J = [0, v_0, ..., v_{T-2}] are
+//   p_j = (J_j - dm1) (J_{j+1} - Dm1),  j = 0 .. T-2,
+// blocked pairwise (block means, java:9308-9316).  One thread per (pixel,
+// segment of 256 products) computes, for levels 0..8, the sums of block means
+// and squared block means of the complete blocks inside its segment, and the
+// segment sum for the higher levels.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) block_kernel(Job j, const void *stack,
+                                                    const float *bparams, const float *basis,
+                                                    const float4 *blkmon, int nbseg,
+                                                    float *s1, float *s2, float *segsum)
+{
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int seg = blockIdx.y;
+    if (pix >= j.npix) return;
+    int xa, ya, xb, yb;
+    trace_origin(j, pix, xa, ya);
+    const int trb = j.is_ccf ? j.npix + pix : pix;
+    trace_origin(j, trb, xb, yb);
+    float bpa[kBleachStride], bpb[kBleachStride];
+    for (int i = 0; i < kBleachStride; i++) {
+        bpa[i] = __ldg(&bparams[(size_t)pix * kBleachStride + i]);
+        bpb[i] = __ldg(&bparams[(size_t)trb * kBleachStride + i]);
+    }
+    const float4 bm = blkmon[pix];   // a1 = dm1 - c0, b1 = Dm1 - c1, dm1, Dm1
+    const int nprod = j.num - 1;
+    const int j0 = seg * kBlkSeg, j1 = min(j0 + kBlkSeg, nprod);
+    float S1[kBlkSegLog + 1], S2[kBlkSegLog + 1], pend[kBlkSegLog + 1];
+    for (int y = 0; y <= kBlkSegLog; y++) { S1[y] = 0.f; S2[y] = 0.f; pend[y] = 0.f; }
+    // direct element of product jj is J_jj = v_{jj-1} (J_0 = 0)
+    float u_prev;
+    if (j0 == 0) u_prev = -bm.z;
+    else u_prev = corrected_delta(j, stack, xa, ya, j0 - 1, bpa, basis) - bm.x;
+    float segv = 0.f;
+    for (int jj = j0; jj < j1; jj++) {
+        float w;
+        if (j.is_ccf) w = corrected_delta(j, stack, xb, yb, jj, bpb, basis) - bm.y;
+        float dcur = j.is_ccf ? 0.f : corrected_delta(j, stack, xa, ya, jj, bpa, basis);
+        if (!j.is_ccf) w = dcur - bm.y;
+        float p = u_prev * w;
+        // next direct element J_{jj+1} = v_jj
+        if (j.is_ccf) u_prev = corrected_delta(j, stack, xa, ya, jj, bpa, basis) - bm.x;
+        else u_prev = dcur - bm.x;
+        int rel = jj - j0;
+        S1[0] += p;
+        S2[0] += p * p;
+        float v = p;
+        int y = 0;
+        while (y < kBlkSegLog && ((rel >> y) & 1)) {
+            v = pend[y] + v;
+            y++;
+            float m = v * (1.f / (float)(1 << y));
+            S1[y] += m;
+            S2[y] += m * m;
+        }
+        if (y < kBlkSegLog) pend[y] = v;
+        else segv = v;
+    }
+    const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
+    for (int y = 0; y <= kBlkSegLog; y++) { s1[o + y] = S1[y]; s2[o + y] = S2[y]; }
+    segsum[(size_t)pix * nbseg + seg] = (j1 - j0 == kBlkSeg) ? segv : nanf("");
+}
+
+// Blocking decision per pixel (one warp): combine segment statistics in FP64,
+// build the levels above the segment size from segment sums, then the
+// overlap / monotonic-increase criteria of java:9339-9380.
+__global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, const float *s2,
+                                      const float *segsum, const float4 *blkmon, int *ind_out,
+                                      int *ok_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int pix = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (pix >= j.npix) return;
+    const int blocknum = j.blocknum;
+    double S1[kMaxBlockLevels], S2[kMaxBlockLevels];
+    for (int y = 0; y < kMaxBlockLevels; y++) { S1[y] = 0.0; S2[y] = 0.0; }
+    for (int seg = lane; seg < nbseg; seg += 32) {
+        const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
+        for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) {
+            S1[y] += s1[o + y];
+            S2[y] += s2[o + y];
+        }
+    }
+    for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) { S1[y] = warp_sum_d(S1[y]); S2[y] = warp_sum_d(S2[y]); }
+    if (lane != 0) return;
+    // levels above the segment: block y spans 2^(y-8) consecutive complete segments
+    for (int y = kBlkSegLog + 1; y < blocknum; y++) {
+        int span = 1 << (y - kBlkSegLog);
+        double inv = 1.0 / (double)(1 << y);
+        for (int b = 0; (b + 1) * span <= nbseg; b++) {
+            double s = 0.0;
+            bool complete = true;
+            for (int k = 0; k < span; k++) {
+                float v = segsum[(size_t)pix * nbseg + b * span + k];
+                if (isnan(v)) { complete = false; break; }
+                s += (double)v;
+            }
+            if (!complete) break;
+            double m = s * inv;
+            S1[y] += m;
+            S2[y] += m * m;
+        }
+    }
+    const float4 bm = blkmon[pix];
+    const double dmDm = (double)bm.z * (double)bm.w;
+    const int nprod = j.num - 1;
+    double vb1[kMaxBlockLevels], upper[kMaxBlockLevels], lower[kMaxBlockLevels];
+    int crt[kMaxBlockLevels] = {0}, cr12[kMaxBlockLevels] = {0}, cr3[kMaxBlockLevels] = {0},
+        diffpos[kMaxBlockLevels] = {0};
+    for (int y = 0; y < blocknum; y++) {
+        double n = (double)(nprod >> y);
+        double v = (S2[y] / n - (S1[y] / n) * (S1[y] / n)) / (n * dmDm * dmDm);
+        vb1[y] = sqrt(v);
+        double e = vb1[y] / sqrt(2 * (n - 1));
+        upper[y] = vb1[y] + e;
+        lower[y] = vb1[y] - e;
+    }
+    for (int x = 0; x < blocknum - 1; x++)
+        if (upper[x] > lower[x + 1] && upper[x + 1] > lower[x]) crt[x] = 1;
+    for (int x = 0; x < blocknum - 2; x++)
+        if (crt[x] * crt[x + 1] == 1) cr12[x] = 1;
+    for (int x = 0; x < blocknum - 1; x++)
+        if (vb1[x + 1] - vb1[x] > 0) diffpos[x] = 1;
+    for (int x = 0; x < blocknum - 2; x++)
+        if (diffpos[x] * diffpos[x + 1] == 1) cr3[x] = 1;
+    int last0 = 0;
+    for (int x = 0; x < blocknum - 2; x++)
+        if (cr3[x] == 1 && cr12[x] == 0) last0 = x;
+    for (int x = 0; x <= last0; x++) cr12[x] = 0;
+    if (blocknum >= 3) cr12[blocknum - 3] = 0;
+    if (blocknum >= 4) cr12[blocknum - 4] = 0;
+    int ind = 0, ok;
+    for (int x = blocknum - 5; x > 0; x--)
+        if (cr12[x] == 1) ind = x + 1;
+    if (ind == 0) {
+        ok = 0;
+        ind = (blocknum - 3 > 0) ? blocknum - 3 : blocknum - 1;
+    } else {
+        ok = 1;
+    }
+    if (ind < q - 1) ind = q - 1;
+    ind_out[pix] = ind;
+    ok_out[pix] = ok;
+}
+
+// Centre of traces whose bleach parameters were supplied by the caller
+// (reference calcACF path): mean of the corrected averaged trace.
+__global__ void center_given_kernel(Job j, const float *trace, float *bp_out)
+{
+    const int lane = threadIdx.x & 31;
+    const int tr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tr >= j.ntrace) return;
+    float *bp = bp_out + (size_t)tr * kBleachStride;
+    const float *y = trace + (size_t)tr * j.nopit;
+    float bpl[kBleachStride];
+    for (int i = 0; i < kBleachStride; i++) bpl[i] = bp[i];
+    float s = 0.f, lb[kMaxPoly + 1];
+    for (int x = lane; x < j.nopit; x += 32) {
+        float v = __ldg(&y[x]);
+        if (j.bleach != IMFCS_BLEACH_NONE && bpl[11] != 0.f) {
+            float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
+            if (j.bleach == IMFCS_BLEACH_POLYNOMIAL) legendre(t * bpl[13] + bpl[14], j.poly_order, lb);
+            v = bleach_correct(v, bleach_f(bpl, j.bleach, j.poly_order, t, lb), bpl[9], bpl[10]);
+        }
+        s += v;
+    }
+    s = warp_sum(s);
+    if (lane == 0) bp[12] = s / j.nopit;
+}
+
+// Stride-1 box-sum binning of a float stack (calc_binning, agpufitjni.cu:4560-4586).
+__global__ void binning_kernel(const float *in, float *out, int win, int hin, int wt, int ht,
+                               int frames, int bx, int by)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)wt * ht * frames;
+    if (i >= n) return;
+    int x = (int)(i % wt);
+    int y = (int)((i / wt) % ht);
+    size_t t = i / ((size_t)wt * ht);
+    const float *f = in + t * (size_t)win * hin;
+    float s = 0.f;
+    for (int a = 0; a < bx; a++)
+        for (int b = 0; b < by; b++) s += f[(size_t)(y + b) * win + x + a];
+    out[i] = s;
+}
+
+// Averages of `ave` frames per pixel of a float stack [t][h][w] -> [h][w][nopit]
+// with the Java CPU's truncating division (java:9852).
+__global__ void bleach_average_kernel(const float *in, float *out, int w, int h, int nopit, int ave)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)w * h * nopit) return;
+    int pix = (int)(i / nopit), x = (int)(i % nopit);
+    double s = 0.0;
+    for (int f = x * ave; f < (x + 1) * ave; f++) s += in[(size_t)f * w * h + pix];
+    out[i] = (float)trunc(s / ave);
+}
+
+// Explicit instantiations used by the host side.
+template __global__ void bleach_exp_kernel<3>(Job, const float *, float *);
+template __global__ void bleach_exp_kernel<5>(Job, const float *, float *);
+
+}  // namespace imfcs
+
+namespace imfcs {
+
+cudaError_t launch_trace(const Job &j, const void *stack, float *trace, cudaStream_t s)
+{
+    dim3 grid((j.ntrace + 31) / 32, (j.nopit + 31) / 32), block(32, 8);
+    trace_kernel<<<grid, block, 0, s>>>(j, stack, trace);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bleach(const Job &j, const float *trace, const double *proj, float uscale,
+                          float uoff, float *bparams, cudaStream_t s)
+{
+    const int threads = 128;
+    const int blocks = (j.ntrace * 32 + threads - 1) / threads;
+    switch (j.bleach) {
+    case IMFCS_BLEACH_POLYNOMIAL:
+        bleach_poly_kernel<<<blocks, threads, 0, s>>>(j, trace, proj, uscale, uoff, bparams);
+        break;
+    case IMFCS_BLEACH_SINGLE_EXP:
+        bleach_exp_kernel<3><<<blocks, threads, 0, s>>>(j, trace, bparams);
+        break;
+    case IMFCS_BLEACH_DOUBLE_EXP:
+        bleach_exp_kernel<5><<<blocks, threads, 0, s>>>(j, trace, bparams);
+        break;
+    default:
+        center_kernel<<<blocks, threads, 0, s>>>(j, trace, bparams);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_center_given(const Job &j, const float *trace, float *bparams, cudaStream_t s)
+{
+    const int threads = 128;
+    center_given_kernel<<<(j.ntrace * 32 + threads - 1) / threads, threads, 0, s>>>(j, trace, bparams);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_monitor(const Job &j, const LagInfo *li_dev, const void *stack,
+                           const float *bparams, const float *basis, const int *snap_pos, int nseg,
+                           float2 *segtot, float2 *snap_part, float4 *mon, float4 *blkmon,
+                           cudaStream_t s)
+{
+    dim3 grid((j.ntrace + 127) / 128, nseg);
+    monitor_kernel<<<grid, 128, 0, s>>>(j, stack, bparams, basis, snap_pos, nseg, segtot, snap_part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int wpb = 4;
+    size_t smem = (size_t)wpb * (nseg + 1 + 2 * j.nsnap) * sizeof(double);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(monitor_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    monitor_finalize_kernel<<<(j.npix + wpb - 1) / wpb, wpb * 32, smem, s>>>(j, li_dev, bparams, nseg,
+                                                                           segtot, snap_part, mon, blkmon);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_block(const Job &j, const void *stack, const float *bparams, const float *basis,
+                         const float4 *blkmon, int nbseg, float *s1, float *s2, float *segsum,
+                         int *ind, int *ok, cudaStream_t s)
+{
+    dim3 grid((j.npix + 127) / 128, nbseg);
+    block_kernel<<<grid, 128, 0, s>>>(j, stack, bparams, basis, blkmon, nbseg, s1, s2, segsum);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    block_finalize_kernel<<<(j.npix * 32 + 127) / 128, 128, 0, s>>>(j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_binning(const float *in, float *out, int win, int hin, int wt, int ht,
+                           int frames, int bx, int by, cudaStream_t s)
+{
+    size_t n = (size_t)wt * ht * frames;
+    binning_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, win, hin, wt, ht, frames, bx, by);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bleach_average(const float *in, float *out, int w, int h, int nopit, int ave,
+                                  cudaStream_t s)
+{
+    size_t n = (size_t)w * h * nopit;
+    bleach_average_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, w, h, nopit, ave);
+    return cudaGetLastError();
+}
+
+}  // namespace imfcs

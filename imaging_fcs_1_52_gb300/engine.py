@@ -1,0 +1,247 @@
+"""Whole-path API over the CUDA library: uint16 stack -> ACF, blocked
+variance, fits, Bayes probabilities, diffusion law.
+
+Device work runs on torch tensors (torch provides device memory and streams;
+the compute is the library's CUDA kernels).  Host work takes numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import NCONST, NPARAM, check
+
+# Plugin defaults (Imaging_FCS_1_52.java:185-205, 1958-1970): N=1, D=1 um^2/s,
+# G=0, everything else 0; N, D, G free.
+DEFAULT_INIT = (1.0, 1e-12, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+DEFAULT_FREE = (1, 1, 0, 0, 1, 0, 0, 0, 0, 0, 0)
+
+
+def obsvol_2d(ax: float, ay: float, s: float) -> float:
+    """Observation area normalisation obsvolFCS_ST2D1p(2) (java:13670-13702), SI."""
+    sqrpi = math.sqrt(3.14159265359)
+    px = s / sqrpi * (2 * math.exp(-(ax / s) ** 2) - 2) + 2 * ax * math.erf(ax / s)
+    py = s / sqrpi * (2 * math.exp(-(ay / s) ** 2) - 2) + 2 * ay * math.erf(ay / s)
+    return 4 * (ax * ay) ** 2 / (px * py)
+
+
+def model_constants(pixel_um: float = 0.24, binx: int = 1, biny: int = 1, psf_um: float = 0.4,
+                    sz_um: float = 1e6 * 0.515 / 1.49, cfx: int = 0, cfy: int = 0,
+                    q2: float = 1.0, q3: float = 1.0) -> np.ndarray:
+    """FCS_3p constants (java:13135-13145, prepareFit 10028-10038) in SI units:
+    ax, ay, s, sz, rx, ry, fitobsvol, q2, q3.  psf_um is the 1/e^2 radius."""
+    ax = pixel_um * 1e-6 * binx
+    ay = pixel_um * 1e-6 * biny
+    s = psf_um * 1e-6
+    rx = ax * cfx / binx
+    ry = ay * cfy / biny
+    return np.array([ax, ay, s, sz_um * 1e-6, rx, ry, obsvol_2d(ax, ay, s), q2, q3], dtype=float)
+
+
+@dataclass
+class FCSConfig:
+    width: int
+    height: int
+    frames: int
+    first: int = 0
+    num: int | None = None
+    out_w: int | None = None
+    out_h: int | None = None
+    map_x0: int = 0
+    map_y0: int = 0
+    binx: int = 1
+    biny: int = 1
+    pixbinx: int | None = None
+    pixbiny: int | None = None
+    cfx: int = 0
+    cfy: int = 0
+    background: int = 0
+    p: int = 16
+    q: int = 8
+    frametime: float = 1e-3
+    bleach: int = _lib.BLEACH_NONE
+    poly_order: int = 4
+    gls: bool = False
+    bayes: bool = False
+    do_fit: bool = True
+    fitstart: int = 1
+    fitend: int | None = None
+    max_iter: int = 2000
+    init: tuple = DEFAULT_INIT
+    free_mask: tuple = DEFAULT_FREE
+    cst: np.ndarray = field(default_factory=model_constants)
+
+    def __post_init__(self):
+        if self.num is None:
+            self.num = self.frames - self.first
+        if self.pixbinx is None:
+            self.pixbinx = self.binx
+        if self.pixbiny is None:
+            self.pixbiny = self.biny
+        if self.out_w is None:
+            self.out_w = (self.width - max(0, self.cfx) - self.binx) // self.pixbinx + 1
+        if self.out_h is None:
+            self.out_h = (self.height - max(0, self.cfy) - self.biny) // self.pixbiny + 1
+
+    @property
+    def chanum(self) -> int:
+        return int(self.p + (self.q - 1) * self.p / 2 + 1)
+
+    @property
+    def npix(self) -> int:
+        return self.out_w * self.out_h
+
+    def to_c(self) -> _lib.Config:
+        c = _lib.Config()
+        for name in ("width", "height", "frames", "first", "num", "out_w", "out_h", "map_x0", "map_y0",
+                     "binx", "biny", "pixbinx", "pixbiny", "cfx", "cfy", "background", "p", "q",
+                     "bleach", "poly_order", "max_iter", "fitstart"):
+            setattr(c, name, int(getattr(self, name)))
+        c.frametime = float(self.frametime)
+        c.gls, c.bayes, c.do_fit = int(self.gls), int(self.bayes), int(self.do_fit)
+        c.fitend = int(self.chanum - 1 if self.fitend is None else self.fitend)
+        for i in range(NPARAM):
+            c.init[i] = float(self.init[i])
+            c.free_mask[i] = int(self.free_mask[i])
+        for i in range(NCONST):
+            c.cst[i] = float(self.cst[i])
+        return c
+
+
+_OUT_SPEC = {  # name -> (dtype, per-pixel shape (function of chanum))
+    "acf": ("f8", lambda c: (c,)), "var": ("f8", lambda c: (c,)), "sd": ("f8", lambda c: (c,)),
+    "blocked_ind": ("i4", lambda c: ()), "blocked_ok": ("i4", lambda c: ()),
+    "nb_mean": ("f8", lambda c: ()), "nb_cov": ("f8", lambda c: ()),
+    "fitres": ("f4", lambda c: (NPARAM,)), "chi2": ("f4", lambda c: ()), "fitted": ("i4", lambda c: ()),
+    "iterations": ("i4", lambda c: ()), "bayes_prob": ("f4", lambda c: (2,)),
+    "covmats": ("f8", lambda c: (c - 1, c - 1)),
+}
+
+
+def output_names(cfg: FCSConfig) -> list[str]:
+    names = ["acf", "var", "sd", "blocked_ind", "blocked_ok", "nb_mean", "nb_cov"]
+    if cfg.do_fit:
+        names += ["fitres", "chi2", "fitted", "iterations"]
+    if cfg.bayes:
+        names += ["bayes_prob"]
+    if cfg.gls:
+        names += ["covmats"]
+    return names
+
+
+def _outputs_struct(ptrs: dict) -> _lib.Outputs:
+    o = _lib.Outputs()
+    for k, v in ptrs.items():
+        setattr(o, k, v)
+    return o
+
+
+class Plan:
+    """A device plan for one configuration (imfcs_plan_*)."""
+
+    def __init__(self, cfg: FCSConfig):
+        self.cfg = cfg
+        self._L = _lib.load()
+        self._c = cfg.to_c()
+        h = C.c_void_p()
+        check(self._L.imfcs_plan_create(C.byref(self._c), C.byref(h)), "imfcs_plan_create")
+        self._h = h
+
+    @property
+    def scratch_bytes(self) -> int:
+        return int(self._L.imfcs_plan_scratch_bytes(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.imfcs_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bleach_params(self) -> np.ndarray:
+        """Per-trace bleach parameters of the last execution (diagnostic)."""
+        n = self.cfg.npix * (2 if (self.cfg.cfx or self.cfg.cfy) else 1)
+        out = np.zeros((n, 16), np.float32)
+        got = self._L.imfcs_plan_bleach_params(self._h, C.c_void_p(out.ctypes.data), n)
+        if got < 0:
+            raise _lib.ImfcsError(_lib.last_error())
+        return out
+
+    def alloc_device_outputs(self, device="cuda"):
+        import torch
+        tmap = {"f8": torch.float64, "f4": torch.float32, "i4": torch.int32}
+        out = {}
+        for n in output_names(self.cfg):
+            dt, shp = _OUT_SPEC[n]
+            out[n] = torch.empty((self.cfg.npix, *shp(self.cfg.chanum)), dtype=tmap[dt], device=device)
+        return out
+
+    def execute(self, stack, outputs: dict, stream=None):
+        """stack: CUDA uint16 tensor [frames][height][width]; outputs: CUDA
+        tensors from alloc_device_outputs.  Asynchronous on `stream`."""
+        import torch
+        assert stack.is_cuda and stack.is_contiguous()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        o = _outputs_struct({k: v.data_ptr() for k, v in outputs.items()})
+        check(self._L.imfcs_plan_execute(self._h, C.c_void_p(stack.data_ptr()), C.byref(o),
+                                         C.c_void_p(s.cuda_stream)), "imfcs_plan_execute")
+        return outputs
+
+    def execute_host(self, stack: np.ndarray, outputs: dict | None = None, stream=None) -> dict:
+        """Host stack in, host results out (copies inside the call)."""
+        stack = np.ascontiguousarray(stack, dtype=np.uint16)
+        if outputs is None:
+            outputs = {}
+            for n in output_names(self.cfg):
+                dt, shp = _OUT_SPEC[n]
+                outputs[n] = np.empty((self.cfg.npix, *shp(self.cfg.chanum)), dtype=dt)
+        o = _outputs_struct({k: v.ctypes.data for k, v in outputs.items()})
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(self._L.imfcs_plan_execute_host(self._h, C.c_void_p(stack.ctypes.data), C.byref(o), sp),
+              "imfcs_plan_execute_host")
+        return outputs
+
+
+def run_host(stack: np.ndarray, cfg: FCSConfig) -> dict:
+    plan = Plan(cfg)
+    try:
+        return plan.execute_host(stack)
+    finally:
+        plan.close()
+
+
+def simulate(width: int, height: int, frames: int, *, frametime: float = 1e-3,
+             steps_per_frame: int = 10, pixel_um: float = 0.24, psf_um: float = 0.4,
+             density: float = 500 / 900.0, d1: float = 1.0, d2: float = 0.0, fraction2: float = 0.0,
+             cps: float = 10000.0, tau_bleach: float = 0.0, offset: int = 100,
+             read_noise: float = 0.0, margin: float = 2.0, seed: int = 1, d_tile_map=None,
+             device="cuda"):
+    """GPU Monte-Carlo stack (imfcs_simulate) as a CUDA uint16 tensor."""
+    import torch
+    L = _lib.load()
+    p = _lib.SimParams(width=width, height=height, frames=frames, frametime=frametime,
+                       steps_per_frame=steps_per_frame, pixel_size=pixel_um, psf_radius=psf_um,
+                       density=density, d1=d1, d2=d2, fraction2=fraction2, cps=cps,
+                       tau_bleach=tau_bleach, offset=offset, read_noise=read_noise, margin=margin,
+                       seed=seed)
+    out = torch.empty((frames, height, width), dtype=torch.uint16, device=device)
+    dmap = None
+    if d_tile_map is not None:
+        dmap = torch.as_tensor(np.ascontiguousarray(d_tile_map, np.float32), device=device)
+    s = torch.cuda.current_stream()
+    check(L.imfcs_simulate(C.byref(p), None if dmap is None else C.c_void_p(dmap.data_ptr()),
+                           C.c_void_p(out.data_ptr()), C.c_void_p(s.cuda_stream)), "imfcs_simulate")
+    return out
+
+
+def to_numpy_u16(t) -> np.ndarray:
+    import torch
+    return t.view(torch.int16).cpu().numpy().view(np.uint16)

@@ -1,0 +1,261 @@
+/*
+ * imfcs_gb300.h -- C ABI of the GB300-native imaging-FCS correlation-and-fit
+ * engine (libimfcs_gb300.so).
+ *
+ * The library replaces the native side of the Imaging_FCS 1.52 plugin's GPU
+ * path: the JNI binding GpufitImFCS.java (class gpufitImFCS.GpufitImFCS) over
+ * libagpufit.so (agpufitjni.cu).  Every reference-facing entry point below
+ * names the Java native method and the agpufitjni.cu implementation it
+ * replaces.  Plain C types only: pointers, sizes and the two parameter
+ * structs.  A JNI shim that forwards the Java natives to these functions is
+ * given in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Return value: 0 = success, nonzero = error; imfcs_get_last_error()
+ *    returns the message of the last failure on the calling thread.
+ *  - "host" pointers are ordinary host memory; "dev" pointers are CUDA device
+ *    pointers of the current device; `stream` is a cudaStream_t (NULL = the
+ *    legacy default stream).
+ *  - No entry point resets the device (the reference ends each call with
+ *    cudaDeviceReset, agpufitjni.cu:4781,4939,5769; on a shared GPU that is
+ *    replaced by freeing this library's own allocations).
+ *  - There is no CPU fallback: without a usable CUDA device every compute
+ *    entry point fails with an error.
+ */
+#ifndef IMFCS_GB300_H
+#define IMFCS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define IMFCS_API __attribute__((visibility("default")))
+#else
+#define IMFCS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMFCS_NPARAM 11 /* N, D, vx, vy, G, F2, D2, F3, D3, Ftrip, Ttrip (SI units) */
+#define IMFCS_NCONST 9  /* ax, ay, s, sz, rx, ry, fitobsvol, q2, q3 (SI units)      */
+
+/* Bleach-correction modes (the plugin's cbBleachCor choices that reach the
+ * correlator: "none", "Single Exp", "Double Exp", "Polynomial"). */
+enum { IMFCS_BLEACH_NONE = 0, IMFCS_BLEACH_SINGLE_EXP = 1,
+       IMFCS_BLEACH_DOUBLE_EXP = 2, IMFCS_BLEACH_POLYNOMIAL = 3 };
+
+/* Fit states, identical to GpufitImFCS.FitState (GpufitImFCS.java:817-866). */
+enum { IMFCS_STATE_CONVERGED = 0, IMFCS_STATE_MAX_ITERATIONS = 1,
+       IMFCS_STATE_SINGULAR_HESSIAN = 2, IMFCS_STATE_NEG_CURVATURE_MLE = 3,
+       IMFCS_STATE_GPU_NOT_READY = 4 };
+
+/* Model ids, identical to GpufitImFCS.Model (GpufitImFCS.java:879-891). */
+enum { IMFCS_MODEL_GAUSS_2D = 1, IMFCS_MODEL_ACF_1D = 2, IMFCS_MODEL_LINEAR_1D = 3 };
+#define IMFCS_ACF_1D_NPARAM 20
+#define IMFCS_LINEAR_1D_NPARAM 11
+
+/* GpufitImFCS.ACFParameters (GpufitImFCS.java:453-486), field for field, in
+ * the plugin's meaning.  Read by the reference at agpufitjni.cu:5462-5504. */
+typedef struct imfcs_acf_parameters {
+    int width, height;          /* output grid */
+    int win_star, hin_star;     /* input width/height of the float stack */
+    int w_temp, h_temp;         /* binned (stride-1 box sum) grid */
+    int pixbinX, pixbinY;
+    int binningX, binningY;
+    int firstframe, lastframe;  /* 1-based, inclusive */
+    int framediff;
+    int cfXDistance, cfYDistance;
+    double correlatorp, correlatorq;
+    double frametime;
+    int background;
+    double mtab1, mtabchanumminus1, sampchanumminus1;
+    int chanum;
+    int isNBcalculation;
+    int bleachcorr_gpu;
+    int bleachcorr_order;       /* number of polynomial coefficients (order + 1) */
+    int nopit, ave;
+} imfcs_acf_parameters;
+
+/* ------------------------------------------------------------------------ */
+/* Device / status (reference-facing).                                       */
+/* ------------------------------------------------------------------------ */
+
+/* GpufitImFCS.isCudaAvailableInt (GpufitImFCS.java:389), agpufitjni.cu:4656.
+ * Returns 1 when a CUDA device of compute capability 10.3 (GB300) is usable. */
+IMFCS_API int imfcs_is_cuda_available(void);
+
+/* GpufitImFCS.getCudaVersionAsArray (GpufitImFCS.java:403), agpufitjni.cu:4668.
+ * Versions as major*1000 + minor*10. */
+IMFCS_API int imfcs_get_cuda_version(int *runtime_version, int *driver_version);
+
+/* GpufitImFCS.getLastError (GpufitImFCS.java:382), agpufitjni.cu:4643. */
+IMFCS_API const char *imfcs_get_last_error(void);
+
+/* GpufitImFCS.resetGPU (GpufitImFCS.java:491), agpufitjni.cu:4692.  Frees the
+ * library's cached device buffers and plans; never resets the device. */
+IMFCS_API int imfcs_reset_gpu(void);
+
+/* ------------------------------------------------------------------------ */
+/* Reference-facing compute entry points (host buffers, synchronous).        */
+/* ------------------------------------------------------------------------ */
+
+/* GpufitImFCS.isBinningMemorySufficient (GpufitImFCS.java:510),
+ * agpufitjni.cu:4816-4853.  Returns 1 / 0. */
+IMFCS_API int imfcs_is_binning_memory_sufficient(const imfcs_acf_parameters *p);
+
+/* GpufitImFCS.calcBinning (GpufitImFCS.java:520), agpufitjni.cu:4860-4967:
+ * stride-1 box sum of binningX x binningY over a float stack
+ * in[t][hin_star][win_star] -> out[t][h_temp][w_temp], frames
+ * firstframe..lastframe. */
+IMFCS_API int imfcs_calc_binning(const float *in, float *out, const imfcs_acf_parameters *p);
+
+/* GpufitImFCS.calcDataBleachCorrection (GpufitImFCS.java:501),
+ * agpufitjni.cu:4708-4810: averages of `ave` frames, out[h][w][nopit], for
+ * the pixels the correlator reads from pixels[t][h_temp][w_temp]. */
+IMFCS_API int imfcs_calc_data_bleach_correction(const float *pixels, float *out,
+                                      const imfcs_acf_parameters *p);
+
+/* GpufitImFCS.isACFmemorySufficient (GpufitImFCS.java:531),
+ * agpufitjni.cu:4974-5092.  Returns 1 / 0. */
+IMFCS_API int imfcs_is_acf_memory_sufficient(const imfcs_acf_parameters *p);
+
+/* GpufitImFCS.calcACF (GpufitImFCS.java:533), agpufitjni.cu:5364-5831.
+ * pixels[t][h_temp][w_temp] (binned, background subtracted), outputs are
+ * lag-major like the reference: pixels1[chanum][height][width] (ACF),
+ * blockvararray[chanum][height][width], NBmean[height][width],
+ * NBcov[height][width], blocked1D[2][height][width] (block index, success
+ * flag).  bleachcorr_params[h_temp][w_temp][bleachcorr_order] are polynomial
+ * coefficients in powers of t (seconds) when bleachcorr_gpu != 0.  samp and
+ * lag receive the lag tables.  Semantics follow the plugin's Java CPU
+ * correlator (java:9124-9648), see the design doc. */
+IMFCS_API int imfcs_calc_acf(const float *pixels, double *pixels1, double *blockvararray,
+                   double *NBmean, double *NBcov, double *blocked1D,
+                   const double *bleachcorr_params, double *samp, int *lag,
+                   const imfcs_acf_parameters *p);
+
+/* GpufitImFCS.fit (GpufitImFCS.java:323), agpufitjni.cu:4614-4640 and the
+ * Gpufit C API gpufit() (agpufitjni.cu:4332-4388).  Models ACF_1D (20
+ * parameters: the 11 FCS parameters then ax, ay, s, sz, rx, ry, fitobsvol,
+ * q2, q3; user_info = n_points float lag times) and LINEAR_1D (polynomial with
+ * num_valid_coefs coefficients; user_info = n_points float abscissae).
+ * Estimator 0 (LSE) only.  Outputs per fit: parameters, state, chi-square
+ * (sum of weighted squared residuals) and iteration count. */
+IMFCS_API int imfcs_fit(int n_fits, int n_points, const float *data, const float *weights,
+              int model_id, const float *initial_parameters, float tolerance,
+              int max_n_iterations, int num_valid_coefs, const int *parameters_to_fit,
+              int estimator_id, size_t user_info_size, const void *user_info,
+              float *output_parameters, int *output_states, float *output_chi_squares,
+              int *output_n_iterations);
+
+/* ------------------------------------------------------------------------ */
+/* GB300-native whole-path API (uint16 stack -> ACF, variance, fits).        */
+/* ------------------------------------------------------------------------ */
+
+/* One correlation job over a raw uint16 stack [frames][height][width]:
+ * output pixel (ox, oy) correlates the binx x biny window at raw
+ * ((map_x0+ox)*pixbinx, (map_y0+oy)*pixbiny) with the window displaced by
+ * (cfx, cfy) (the correlateROI CPU loop, java:8457-8556). */
+typedef struct imfcs_config {
+    int width, height, frames;   /* raw stack geometry */
+    int first, num;              /* 0-based first frame, number of frames */
+    int out_w, out_h, map_x0, map_y0;
+    int binx, biny, pixbinx, pixbiny;
+    int cfx, cfy;
+    int background;              /* counts per raw pixel (java getIntensity) */
+    int p, q;                    /* correlator: P = 16, Q >= 1 (chanum = P+(Q-1)P/2+1) */
+    double frametime;            /* seconds */
+    int bleach, poly_order;      /* IMFCS_BLEACH_*, polynomial order 1..8 */
+    int gls, bayes, do_fit;      /* GLS covariance/fit, Bayes 1-vs-2, fit at all */
+    int fitstart, fitend;        /* OLS fit range (lag indices), java:10358-10369 */
+    int max_iter;                /* LM iteration cap (java:199: 2000) */
+    double init[IMFCS_NPARAM];   /* initial values (SI) */
+    int free_mask[IMFCS_NPARAM]; /* 1 = fitted, 0 = held at init */
+    double cst[IMFCS_NCONST];    /* model constants (SI) */
+} imfcs_config;
+
+/* Output buffers of a job ([pixel][...] with pixel = oy*out_w + ox).
+ * Any pointer may be NULL to skip that output. */
+typedef struct imfcs_outputs {
+    double *acf;         /* [npix][chanum]  (GLS: mcov, as java:9638-9642)    */
+    double *var;         /* [npix][chanum]  blocked variance                 */
+    double *sd;          /* [npix][chanum]                                   */
+    int *blocked_ind;    /* [npix] blocking index                            */
+    int *blocked_ok;     /* [npix] blockIndS                                 */
+    double *nb_mean;     /* [npix] lag-1 direct monitor (N&B)                */
+    double *nb_cov;      /* [npix] lag-1 covariance (N&B)                    */
+    float *fitres;       /* [npix][11] fitted parameters (SI), NaN if failed */
+    float *chi2;         /* [npix] reduced chi-square as java:10403-10406    */
+    int *fitted;         /* [npix] 1 if the fit succeeded                    */
+    int *iterations;     /* [npix] LM iterations                             */
+    float *bayes_prob;   /* [npix][2] model probabilities (1 and 2 comp.)    */
+    double *covmats;     /* [npix][(chanum-1)^2] regularised covariance (GLS) */
+} imfcs_outputs;
+
+/* Number of correlation channels for (p, q): p + (q-1)*p/2 + 1. */
+IMFCS_API int imfcs_chanum(int p, int q);
+
+/* Plans hold the device scratch of one configuration; create once, execute
+ * many times.  Not thread-safe per plan. */
+typedef struct imfcs_plan imfcs_plan;
+IMFCS_API int imfcs_plan_create(const imfcs_config *cfg, imfcs_plan **plan);
+IMFCS_API int imfcs_plan_destroy(imfcs_plan *plan);
+/* Bytes of device scratch the plan holds. */
+IMFCS_API size_t imfcs_plan_scratch_bytes(const imfcs_plan *plan);
+
+/* Diagnostic (no counterpart in the reference): copies the per-trace bleach
+ * parameters of the last execution to host memory, 16 floats per trace
+ * ([0..8] fit coefficients, [9] f0, [11] valid flag, [12] centre).  Returns
+ * the number of traces. */
+IMFCS_API int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out, int max_traces);
+
+/* Runs the whole path on a device-resident stack; outputs are device
+ * pointers.  Asynchronous on `stream`. */
+IMFCS_API int imfcs_plan_execute(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,
+                       void *stream);
+
+/* Same path with host buffers: copies the stack (host, ideally pinned) in,
+ * runs, copies the outputs back and synchronises. */
+IMFCS_API int imfcs_plan_execute_host(imfcs_plan *plan, const uint16_t *host_stack,
+                            const imfcs_outputs *host_out, void *stream);
+
+/* FCS diffusion law (dlfit, java:11007-11231, determineDiffusionLaw 8190-8250,
+ * fitDiffLaw 8253-8295): for binnings 1..n_bin the whole path is run on the
+ * device-resident stack; out[3*n_bin] = {Aeff [um^2], mean D [um^2/s],
+ * variance of D} per binning, line[2] = intercept, slope of Aeff/D vs Aeff
+ * fitted over binnings fit_lo..fit_hi (1-based).  `cfg` supplies everything
+ * except the binning and output grid, which follow the "All", non-overlap
+ * mode of the plugin. */
+IMFCS_API int imfcs_diffusion_law(const imfcs_config *cfg, const uint16_t *dev_stack, int n_bin,
+                        int fit_lo, int fit_hi, double pixel_size_m, double psf_m,
+                        double *out, double *line, void *stream);
+
+/* Seeded 2D Brownian-motion stack simulator (semantics of simulateACF2D,
+ * java:13854-14409: Brownian steps, Gaussian PSF photon scatter, Poisson
+ * emission, camera offset).  Writes dev_stack[frames][height][width].
+ * d_tile_map (optional, [ceil(h/16)][ceil(w/16)] um^2/s) gives D per 16x16
+ * pixel tile; fraction2/d2 add a second species; tau_bleach (s, 0 = none)
+ * bleaches the emission exponentially. */
+typedef struct imfcs_sim_params {
+    int width, height, frames;
+    double frametime;            /* s */
+    int steps_per_frame;
+    double pixel_size;           /* um, object space */
+    double psf_radius;           /* 1/e^2 radius, um */
+    double density;              /* particles per um^2 */
+    double d1, d2, fraction2;    /* um^2/s */
+    double cps;                  /* photons per second per particle */
+    double tau_bleach;           /* s */
+    int offset;                  /* camera offset, counts */
+    double read_noise;           /* Gaussian read noise sigma, counts */
+    double margin;               /* um around the detector */
+    uint64_t seed;
+} imfcs_sim_params;
+IMFCS_API int imfcs_simulate(const imfcs_sim_params *sp, const float *dev_d_tile_map, uint16_t *dev_stack,
+                   void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
