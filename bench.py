@@ -1,0 +1,304 @@
+"""Benchmark: ACF + fit pixels/s on a 128 x 128 x 50,000-frame uint16 stack.
+
+Workload (the plain method at scale): a seeded 2D Brownian simulation
+(GPU Monte-Carlo, D drawn per 16 x 16 tile from U(0.2, 5) um^2/s,
+single-exponential bleach tau = 20 s, 500 particles per 30 x 30 um, PSF
+1/e^2 radius 0.4 um, 10,000 photons/s per particle, offset 100), all-pixel
+multi-tau ACFs (P=16, Q=8, 73 channels) with blocked variance,
+single-exponential bleach correction, and a batched LM fit of the TIRF
+one-component model (N, D, G free) of every pixel.
+
+One step = the whole path over the full stack.  `value` is measured with the
+stack resident in HBM (1.64 GB, larger than L2, so no flush is needed);
+`e2e` goes through the C ABI with host buffers (imfcs_plan_execute_host:
+pinned host stack -> device, run, results -> host) every step.
+
+--impl reference runs the reference's CPU implementation of the path: the
+Java CPU code cannot run here (no JVM), so the FP64 C restatement in oracle/
+stands in for it, with all host threads (OpenMP), on a bounded sample of the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 128
+T = 50000
+METRIC = "ACF+fit pixels/s at 128²×50k frames"
+UNIT = "pixels/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=0, help="pixels in the CPU baseline sample (0: auto)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_config(engine, lib):
+    return engine.FCSConfig(width=W, height=H, frames=T, background=100, bleach=lib.BLEACH_SINGLE_EXP,
+                            p=16, q=8, frametime=1e-3, do_fit=True,
+                            cst=engine.model_constants(pixel_um=0.24, psf_um=0.4))
+
+
+def simulate_stack(engine, seed):
+    rng = np.random.default_rng(seed)
+    dmap = rng.uniform(0.2, 5.0, (H // 16, W // 16)).astype(np.float32)
+    return engine.simulate(W, H, T, frametime=1e-3, steps_per_frame=10, pixel_um=0.24, psf_um=0.4,
+                           density=500 / 900.0, cps=10000.0, tau_bleach=20.0, offset=100,
+                           margin=2.0, seed=seed, d_tile_map=dmap)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and "Active" in r[3 + i]
+                          and "Not" not in r[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_profile_traffic():
+    """DRAM bytes per correlator launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "corr_kernel_traffic.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["bytes_per_launch_full_size"])
+        except Exception:
+            return None
+    return None
+
+
+def cpu_baseline(stack_np, cfg, sample_pixels, threads):
+    """The FP64 oracle (restatement of the Java CPU path) on a bounded sample
+    of the same workload: sample_pixels pixels of one row band, all frames."""
+    import oracle  # checker / baseline only
+    ncols = min(sample_pixels, W)
+    nrows = max(1, sample_pixels // ncols)
+    sub = np.ascontiguousarray(stack_np[:, :nrows, :ncols])
+    t0 = time.perf_counter()
+    oracle.run(sub, out_w=ncols, out_h=nrows, background=cfg.background, p=cfg.p, q=cfg.q,
+               frametime=cfg.frametime, bleach=cfg.bleach, init=np.array(cfg.init),
+               free_mask=np.array(cfg.free_mask, np.int32), cst=cfg.cst, threads=threads)
+    dt = time.perf_counter() - t0
+    return ncols * nrows / dt, ncols * nrows, dt
+
+
+def reference_arm(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    from imaging_fcs_1_52_gb300 import engine, _lib  # config + synthetic data only
+    cfg = make_config(engine, _lib)
+    stack_np = None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            stack_np = engine.to_numpy_u16(simulate_stack(engine, seed=1)[:, :8, :].contiguous())
+    except Exception:
+        stack_np = None
+    if stack_np is None:
+        from tests.synth import brownian_stack
+        stack_np = brownian_stack(W, 8, T, seed=1, tau_bleach=20.0)
+    sample = args.cpu_sample or 128
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, n, dt = cpu_baseline(stack_np, cfg, sample, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sample / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "128x128x50000 uint16, single-exp bleach, P=16 Q=8, "
+                                            "OLS LM TIRF fit", "sample": f"{sample} pixels x 50000 frames"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{sample} pixels x 50000 frames, FP64 C restatement of the Java CPU path"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from imaging_fcs_1_52_gb300 import _lib, engine
+
+    cfg = make_config(engine, _lib)
+    stack = simulate_stack(engine, seed=1 + rank)        # each rank: its own stack (weak scaling)
+    torch.cuda.synchronize()
+    plan = engine.Plan(cfg)
+    plan.set_timing(True)
+    out = plan.alloc_device_outputs()
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        plan.execute(stack, out)
+    barrier()
+    corr_ms = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        stage_acc = None
+        for _ in range(args.steps):
+            plan.execute(stack, out)
+            torch.cuda.synchronize()     # stage events of this step are then readable
+            st = plan.stage_times()
+            corr_ms.append(st["correlator"])
+            stage_acc = st if stage_acc is None else {k: stage_acc[k] + st[k] for k in st}
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cfg.npix / (ms * 1e-3)
+
+    # e2e through the C ABI with host buffers (pinned host stack)
+    host = torch.empty((T, H, W), dtype=torch.int16, pin_memory=True)
+    host.copy_(stack.view(torch.int16).cpu())
+    host_np = host.numpy().view(np.uint16)
+    outs_host = {}
+    for n in engine.output_names(cfg):
+        dt, shp = engine._OUT_SPEC[n]
+        outs_host[n] = np.empty((cfg.npix, *shp(cfg.chanum)), dtype=dt)
+    plan.execute_host(host_np, outs_host)           # warm-up of the host path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.execute_host(host_np, outs_host)
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = T * H * W * 2
+    d2h = sum(v.nbytes for v in outs_host.values())
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        corr_avg = statistics.mean(corr_ms)
+        # algorithmic bytes of one correlator launch: the uint16 stack once +
+        # ACF and blocked variance out (8 B each per pixel and channel)
+        alg_bytes = T * H * W * 2 + cfg.npix * cfg.chanum * 8 * 2
+        achieved = alg_bytes / (corr_avg * 1e-3) / 1e9
+        sample = args.cpu_sample or 64
+        stack_np = engine.to_numpy_u16(stack[:, :1, :].contiguous())
+        cpu_v, cpu_n, cpu_dt = cpu_baseline(stack_np, cfg, sample, os.cpu_count() or 1)
+        fitted = int(out["fitted"].sum().item())
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU Monte-Carlo, seeded)",
+            "config": {"workload": "128x128x50000 uint16 stack; single-exp bleach; P=16 Q=8 (73 ch); "
+                                   "blocked variance; OLS LM TIRF fit (N, D, G)",
+                       "pixels_per_rank": cfg.npix, "frames": T, "l2": "inputs 1.64 GB > L2, no flush needed",
+                       "parallelism": f"pixel shards x{world}", "fitted_pixels": fitted},
+            "e2e": {"value": world * cfg.npix / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": 12 * args.steps,
+            "stages_ms": {k: v / args.steps for k, v in stage_acc.items()},
+            "roofline": {"kernel": "corr_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": load_profile_traffic(),
+                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": corr_avg},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"{cpu_n} pixels x 50000 frames of the same stack, FP64 C oracle, "
+                                       f"{cpu_dt:.1f} s"},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

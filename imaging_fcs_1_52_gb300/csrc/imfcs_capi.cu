@@ -256,10 +256,23 @@ struct imfcs_plan {
     uint16_t *dstack = nullptr;
     imfcs_outputs dout;
     bool dout_alloc = false;
+    // stage timing
+    static constexpr int kStages = 6;
+    bool timing = false;
+    cudaEvent_t ev[kStages + 1] = {};
+    bool ev_used[kStages + 1] = {};
     ~imfcs_plan()
     {
         for (auto &b : bufs) cudaFree(b.p);
         if (li_dev) cudaFree(li_dev);
+        for (int i = 0; i <= kStages; i++)
+            if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+    void mark(int i, cudaStream_t s)
+    {
+        if (!timing) return;
+        cudaEventRecord(ev[i], s);
+        ev_used[i] = true;
     }
     template <class T>
     cudaError_t alloc(T *&ptr, size_t count)
@@ -548,18 +561,24 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     const int chanum = pl->chanum;
     double *acf = dev_out->acf ? dev_out->acf : pl->acf_int;
     double *var = dev_out->var ? dev_out->var : pl->var_int;
+    for (int i = 0; i <= imfcs_plan::kStages; i++) pl->ev_used[i] = false;
+    pl->mark(0, s);
     CK(launch_trace(j, dev_stack, pl->trace, s));
     if (pl->given_bleach) CK(launch_center_given(j, pl->trace, pl->bparams, s));
     else CK(launch_bleach(j, pl->trace, pl->proj, (float)pl->uscale, (float)pl->uoff, pl->bparams, s));
+    pl->mark(1, s);
     CK(launch_monitor(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->snap_pos, pl->nseg,
                       pl->segtot, pl->snap_part, pl->mon, pl->blkmon, s));
+    pl->mark(2, s);
     CK(launch_block(j, dev_stack, pl->bparams, pl->basis, pl->blkmon, pl->nbseg, pl->s1, pl->s2,
                     pl->segsum, pl->blk_ind, pl->blk_ok, s));
+    pl->mark(3, s);
     CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->mon, pl->blk_ind, acf, var,
                    dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats,
                    c.gls, s));
     if (dev_out->blocked_ind) CK(cudaMemcpyAsync(dev_out->blocked_ind, pl->blk_ind, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     if (dev_out->blocked_ok) CK(cudaMemcpyAsync(dev_out->blocked_ok, pl->blk_ok, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
+    pl->mark(4, s);
     if (c.gls) {
         GlsArgs g;
         memset(&g, 0, sizeof(g));
@@ -576,6 +595,7 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
         g.covmats_out = dev_out->covmats;
         CK(launch_gls(g, s));
     }
+    pl->mark(5, s);
     if (c.do_fit || c.bayes) {
         const float *y = c.gls ? pl->ytrans : pl->fit_y;
         const float *w = c.gls ? nullptr : pl->fit_w;
@@ -597,6 +617,7 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
             if (dev_out->bayes_prob) CK(launch_bayes_combine(pl->npix, pl->logp1, pl->logp2, dev_out->bayes_prob, s));
         }
     }
+    pl->mark(6, s);
     return 0;
 }
 }  // namespace imfcs
@@ -794,5 +815,28 @@ extern "C" int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out,
     int n = plan->job.ntrace < max_traces ? plan->job.ntrace : max_traces;
     cudaError_t e = cudaMemcpy(host_out, plan->bparams, sizeof(float) * kBleachStride * n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { set_error(cuda_msg(e, "bleach params")); return -1; }
+    return n;
+}
+
+extern "C" int imfcs_plan_set_timing(imfcs_plan *plan, int enable)
+{
+    if (!plan) { set_error("null plan"); return 1; }
+    if (enable && !plan->ev[0])
+        for (int i = 0; i <= imfcs_plan::kStages; i++) CK(cudaEventCreate(&plan->ev[i]));
+    plan->timing = enable != 0;
+    return 0;
+}
+
+extern "C" int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max_stages)
+{
+    if (!plan || !ms) { set_error("null argument"); return -1; }
+    int n = max_stages < imfcs_plan::kStages ? max_stages : imfcs_plan::kStages;
+    for (int i = 0; i < n; i++) {
+        ms[i] = 0.f;
+        if (plan->ev_used[i] && plan->ev_used[i + 1]) {
+            cudaError_t e = cudaEventElapsedTime(&ms[i], plan->ev[i], plan->ev[i + 1]);
+            if (e != cudaSuccess) { set_error(cuda_msg(e, "cudaEventElapsedTime")); return -1; }
+        }
+    }
     return n;
 }

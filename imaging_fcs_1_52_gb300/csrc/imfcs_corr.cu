@@ -91,11 +91,95 @@ __device__ __noinline__ void block_head_init(float *head_sm, const float *wsm)
     for (int d = 1; d <= kP; d++) { h += wsm[(d - 1) * 32]; head_sm[d * 32] = h; }
 }
 
+// One branch-free group of 16 direct samples (positions i0..i0+15) with the
+// delayed samples in a register ring: w[(PH + j + d) & 31] holds position
+// i0 + j + d.  Loads the delayed samples of the next group on the way.
+template <int NL, int DEL0, int PH>
+__device__ __forceinline__ void group16(const float *buf0, const float *buf1, int i0, float (&w)[32],
+                                        float *acc, float &B0, float &B1)
+{
+#pragma unroll
+    for (int jj = 0; jj < 16; jj++) {
+        const int i = i0 + jj;
+        w[(PH + jj + kP) & 31] = buf1[(i + kP) * 32];
+        const float x0 = buf0[i * 32];
+#pragma unroll
+        for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, w[(PH + jj + DEL0 + l) & 31], acc[l]);
+        B0 += x0;
+        B1 += w[(PH + jj) & 31];
+    }
+}
+
+// Generic per-sample path (range checks, first-block heads, block ends at
+// any sample); used where a group is not entirely regular.
+template <int NL, int DEL0>
+__device__ __forceinline__ void samples_slow(const Job &j, const CorrOut &o, const float4 *mon, int pix,
+                                             int lagbase, const float *buf0, const float *buf1, int i0,
+                                             int i1, int ybeg, int numbin, int L, int pnum, float *acc,
+                                             float &B0, float &B1, float *head_sm)
+{
+    for (int i = i0; i < i1; i++) {
+        const int y = ybeg + i;
+        if (y < 0 || y >= numbin) continue;
+        const float x0 = buf0[i * 32];
+        if (y == 0) block_head_init(head_sm, buf1 + i * 32);
+#pragma unroll
+        for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, buf1[(i + DEL0 + l) * 32], acc[l]);
+        B0 += x0;
+        B1 += buf1[i * 32];
+        if ((y & (L - 1)) == L - 1) {
+            float tmp[NL];
+#pragma unroll
+            for (int l = 0; l < NL; l++) tmp[l] = acc[l];
+            block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i + 1) * 32, y / L, L,
+                      pnum);
+#pragma unroll
+            for (int l = 0; l < NL; l++) acc[l] = 0.f;
+            B0 = 0.f;
+            B1 = 0.f;
+        }
+    }
+}
+
+// One group of 16 samples at ring phase PH: fast path when, for every lane,
+// the group lies inside [1, numbin) and blocks are at least 16 long (then a
+// block can only end on the group's last sample, y = 16m + 15).
+template <int NL, int DEL0, int PH>
+__device__ __forceinline__ void group_step(const Job &j, const CorrOut &o, const float4 *mon, int pix,
+                                           int lagbase, const float *buf0, const float *buf1, int i0,
+                                           int ybeg, int numbin, int L, int pnum, float (&w)[32],
+                                           float *acc, float &B0, float &B1, float *head_sm)
+{
+    const int y0 = ybeg + i0, y1 = y0 + 15;
+    const bool fast = (y0 >= 1) && (y1 < numbin) && (L >= 16);
+    if (__all_sync(0xffffffffu, fast)) {
+        group16<NL, DEL0, PH>(buf0, buf1, i0, w, acc, B0, B1);
+        if ((y1 & (L - 1)) == L - 1) {
+            float tmp[NL];
+#pragma unroll
+            for (int l = 0; l < NL; l++) tmp[l] = acc[l];
+            block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i0 + 16) * 32, y1 / L,
+                      L, pnum);
+#pragma unroll
+            for (int l = 0; l < NL; l++) acc[l] = 0.f;
+            B0 = 0.f;
+            B1 = 0.f;
+        }
+    } else {
+        samples_slow<NL, DEL0>(j, o, mon, pix, lagbase, buf0, buf1, i0, i0 + 16, ybeg, numbin, L, pnum, acc,
+                               B0, B1, head_sm);
+        // keep the ring valid for the next group (positions i0+16..i0+31)
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) w[(PH + 16 + jj) & 31] = buf1[(i0 + 16 + jj) * 32];
+    }
+}
+
 // Process the direct samples of one level held in shared memory.
 // buf0/buf1: level buffers (already offset by lane), [kHist + nnew] x 32;
 // position i holds sample s_begin - kHist + i.  Direct samples are
-// positions [0, nnew).
-template <int NL, int DEL0, bool RING>
+// positions [0, nnew).  GROUPED requires nnew % 16 == 0 (s_begin is then a
+// multiple of 16, so groups start at y = 16m).
+template <int NL, int DEL0, bool GROUPED>
 __device__ __forceinline__ void correlate_level(const Job &j, const CorrOut &o, const float4 *mon,
                                                 int pix, int lagbase, const float *buf0,
                                                 const float *buf1, int nnew, int s_begin, int numbin,
@@ -104,59 +188,20 @@ __device__ __forceinline__ void correlate_level(const Job &j, const CorrOut &o, 
 {
     const int ybeg = s_begin - kHist;
     if (ybeg >= numbin || ybeg + nnew <= 0) return;
-    if (RING) {
-        // register ring of delayed samples: w[(i + d) & 31] = buf1[i + d]
+    if (GROUPED) {
         float w[32];
 #pragma unroll
         for (int d = 0; d < kP; d++) w[d] = buf1[d * 32];
-        for (int base = 0; base < nnew; base += 32) {
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) {
-                const int i = base + jj;
-                w[(jj + kP) & 31] = buf1[(i + kP) * 32];
-                const float x0 = buf0[i * 32];
-                const int y = ybeg + i;
-                if (y < 0 || y >= numbin) continue;
-                if (y == 0) block_head_init(head_sm, buf1 + i * 32);
-#pragma unroll
-                for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, w[(jj + DEL0 + l) & 31], acc[l]);
-                B0 += x0;
-                B1 += w[jj & 31];
-                if ((y & (L - 1)) == L - 1) {
-                    float tmp[NL];
-#pragma unroll
-                    for (int l = 0; l < NL; l++) tmp[l] = acc[l];
-                    block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i + 1) * 32,
-                              y / L, L, pnum);
-#pragma unroll
-                    for (int l = 0; l < NL; l++) acc[l] = 0.f;
-                    B0 = 0.f;
-                    B1 = 0.f;
-                }
-            }
+        for (int g = 0; g < nnew; g += 32) {
+            group_step<NL, DEL0, 0>(j, o, mon, pix, lagbase, buf0, buf1, g, ybeg, numbin, L, pnum, w, acc, B0, B1,
+                                    head_sm);
+            if (g + 16 < nnew)
+                group_step<NL, DEL0, 16>(j, o, mon, pix, lagbase, buf0, buf1, g + 16, ybeg, numbin, L, pnum, w,
+                                         acc, B0, B1, head_sm);
         }
     } else {
-        for (int i = 0; i < nnew; i++) {
-            const int y = ybeg + i;
-            if (y < 0 || y >= numbin) continue;
-            const float x0 = buf0[i * 32];
-            if (y == 0) block_head_init(head_sm, buf1 + i * 32);
-#pragma unroll
-            for (int l = 0; l < NL; l++) acc[l] = fmaf(x0, buf1[(i + DEL0 + l) * 32], acc[l]);
-            B0 += x0;
-            B1 += buf1[i * 32];
-            if ((y & (L - 1)) == L - 1) {
-                float tmp[NL];
-#pragma unroll
-                for (int l = 0; l < NL; l++) tmp[l] = acc[l];
-                block_end(j, o, mon, pix, lagbase, DEL0, NL, tmp, B0, B1, head_sm, buf1 + (i + 1) * 32,
-                          y / L, L, pnum);
-#pragma unroll
-                for (int l = 0; l < NL; l++) acc[l] = 0.f;
-                B0 = 0.f;
-                B1 = 0.f;
-            }
-        }
+        samples_slow<NL, DEL0>(j, o, mon, pix, lagbase, buf0, buf1, 0, nnew, ybeg, numbin, L, pnum, acc, B0,
+                               B1, head_sm);
     }
 }
 
@@ -330,7 +375,7 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
                     float *hs = st + 10 * 32 + lane;
                     const int L = 1 << (ind - k);
                     const int lagbase = (kP + 1) + (k - 1) * 8;
-                    if (nk >= 32)
+                    if (nk >= 16)
                         correlate_level<8, 9, true>(j, o, mon, pix, lagbase, buf0 + level_off(k) + lane,
                                                     buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
                                                     B0, B1, hs);

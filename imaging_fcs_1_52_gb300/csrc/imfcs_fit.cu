@@ -9,8 +9,8 @@
 // Lanes own fit points; J^T W J, J^T W r and chi^2 are warp reductions; the
 // small K x K damped system is solved redundantly in every lane.  The grid is
 // persistent: each warp strides over fits.  The solver stops on a small step
-// (|h_i| <= 1e-6 |p_i| + 1e-4 sigma_i), which pins the minimum to ~1e-6 sigma
-// in FP32, or on the Gpufit criterion |dchi2| < tol max(1, chi2) when a
+// (undamped Gauss-Newton step |h_i| <= 1e-6 |p_i| + 1e-5 sigma_i), which pins
+// the minimum to ~1e-5 sigma in FP32, or when no step lowers chi^2 any more, or on the Gpufit criterion |dchi2| < tol max(1, chi2) when a
 // tolerance is given through the reference fit API.
 #include <math.h>
 
@@ -256,6 +256,23 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
         else if (a.k == 0) state = IMFCS_STATE_CONVERGED;
         for (it = 0; state == IMFCS_STATE_MAX_ITERATIONS && it < a.max_iter; it++) {
             float h[KM];
+            if (a.tol <= 0.f) {
+                // converged when the undamped Gauss-Newton step is negligible:
+                // |h_i| <= 1e-6 |p_i| + 1e-5 sigma_i (sigma_i = 1/sqrt(A_ii))
+                float hg[KM], zero[KM];
+#pragma unroll
+                for (int i = 0; i < KM; i++) zero[i] = 0.f;
+                if (chol_solve_f<KM>(s.A, s.g, a.k, 0.f, zero, hg)) {
+                    bool conv = true;
+#pragma unroll
+                    for (int i = 0; i < KM; i++)
+                        if (i < a.k) {
+                            float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
+                            conv = conv && (fabsf(hg[i]) <= 1e-6f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
+                        }
+                    if (conv) { state = IMFCS_STATE_CONVERGED; break; }
+                }
+            }
             if (!chol_solve_f<KM>(s.A, s.g, a.k, lambda, dscale, h)) {
                 lambda *= 10.f;
                 if (lambda > 1e15f) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
@@ -291,15 +308,14 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                 if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
                 if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
             } else {
-                bool accept = finite && (sn.chi2 < s.chi2 || (small && sn.chi2 <= s.chi2 * (1.f + 4e-7f)));
-                if (accept) {
+                if (finite && sn.chi2 < s.chi2) {
                     for (int i = 0; i < a.np; i++) par[i] = pn[i];
                     s = sn;
                     lambda = fmaxf(lambda * 0.1f, 1e-9f);
 #pragma unroll
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) dscale[i] = fmaxf(dscale[i], s.A[i * KM + i]);
-                    if (small) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                    (void)small;
                 } else {
                     lambda *= 10.f;
                     if (lambda > 1e12f) { state = IMFCS_STATE_CONVERGED; it++; break; }

@@ -136,6 +136,27 @@ __device__ __forceinline__ int window_value_int(const Job &j, const void *stack,
     }
 }
 
+// N consecutive frames t..t+N-1 of one window (frames >= tmax read as 0).
+// The loads are issued back to back so that a thread keeps N requests in
+// flight (the streaming passes are latency-bound otherwise).
+template <int N>
+__device__ __forceinline__ void window_values(const Job &j, const void *stack, int x0, int y0, int t,
+                                              int tmax, float *v)
+{
+    const size_t fsz = (size_t)j.in_w * j.in_h;
+    if (!j.input_float && j.binx == 1 && j.biny == 1) {
+        const uint16_t *s = (const uint16_t *)stack + (size_t)j.first * fsz + (size_t)y0 * j.in_w + x0;
+        unsigned short r[N];
+#pragma unroll
+        for (int u = 0; u < N; u++) r[u] = (t + u < tmax) ? __ldg(&s[(size_t)(t + u) * fsz]) : (unsigned short)j.background;
+#pragma unroll
+        for (int u = 0; u < N; u++) v[u] = (float)((int)r[u] - j.background);
+    } else {
+#pragma unroll
+        for (int u = 0; u < N; u++) v[u] = (t + u < tmax) ? window_value(j, stack, x0, y0, t + u) : 0.f;
+    }
+}
+
 __device__ __forceinline__ void trace_origin(const Job &j, int trace, int &x0, int &y0)
 {
     int pix = trace < j.npix ? trace : trace - j.npix;

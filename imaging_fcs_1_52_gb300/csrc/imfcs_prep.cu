@@ -32,7 +32,13 @@ __global__ void __launch_bounds__(256) trace_kernel(Job j, const void *stack, fl
         float val = 0.f;
         if (valid && x < j.nopit) {
             int sum = 0;
-            for (int f = x * j.ave; f < (x + 1) * j.ave; f++) sum += window_value_int(j, stack, x0, y0, f);
+            const int fb = x * j.ave, fe = (x + 1) * j.ave;
+            for (int f = fb; f < fe; f += 8) {
+                float v[8];
+                window_values<8>(j, stack, x0, y0, f, fe, v);
+#pragma unroll
+                for (int u = 0; u < 8; u++) sum += (int)v[u];
+            }
             val = (float)(sum / j.ave);
         }
         tile[tx][xl] = val;
@@ -221,10 +227,24 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     chi2 = accumulate(p, A, g);
     if (!isfinite(chi2)) ok = false;
     int it_n = 0;
-    for (it_n = 0; ok && it_n < 500; it_n++) {
+    for (it_n = 0; ok && it_n < 300; it_n++) {
         float M[K * K], h[K], pn[K];
+        float dmax = 0.f;
+        for (int a = 0; a < K; a++) dmax = fmaxf(dmax, A[a * K + a]);
+        // converged when the undamped Gauss-Newton step is negligible
+        {
+            for (int a = 0; a < K * K; a++) M[a] = A[a];
+            for (int a = 0; a < K; a++) M[a * K + a] += 1e-12f * dmax;
+            if (solve_spd<K>(M, g, h)) {
+                bool conv = true;
+                for (int a = 0; a < K; a++) conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(p[a]) + 1e-6f;
+                if (conv) break;
+            }
+        }
         for (int a = 0; a < K * K; a++) M[a] = A[a];
-        for (int a = 0; a < K; a++) M[a * K + a] *= (1.f + lambda);
+        // Marquardt damping with a floor so that a zero column (e.g. a zero
+        // initial amplitude) still gives a solvable system
+        for (int a = 0; a < K; a++) M[a * K + a] += lambda * fmaxf(A[a * K + a], 1e-6f * dmax);
         if (!solve_spd<K>(M, g, h)) { lambda *= 10.f; if (lambda > 1e20f) break; continue; }
         float rel = 0.f;
         for (int a = 0; a < K; a++) {
@@ -233,13 +253,12 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         }
         float An[K * K], gn[K];
         float c2n = accumulate(pn, An, gn);
-        if (isfinite(c2n) && c2n <= chi2) {
-            float dec = (chi2 - c2n) / fmaxf(chi2, 1e-30f);
+        if (isfinite(c2n) && c2n < chi2) {
             for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
             for (int a = 0; a < K * K; a++) A[a] = An[a];
             chi2 = c2n;
-            lambda = fmaxf(lambda * 0.1f, 1e-7f);
-            if (dec < 1e-7f && rel < 1e-5f) break;
+            lambda = fmaxf(lambda * 0.1f, 1e-9f);
+            (void)rel;
         } else {
             lambda *= 10.f;
             if (lambda > 1e12f) break;
@@ -285,6 +304,18 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
 // Corrected, centred frame value of a trace (the value the correlator uses).
 // basis: Legendre table [num][order+1] for the polynomial mode.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float correct_value(const Job &j, float v, int t, const float *bp,
+                                               const float *basis)
+{
+    if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
+        float tt = (float)(j.frametime_d * (t + 1.5));
+        float f = bleach_f(bp, j.bleach, j.poly_order, tt,
+                           basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
+        v = bleach_correct(v, f, bp[9], bp[10]);
+    }
+    return v - bp[12];
+}
+
 __device__ __forceinline__ float corrected_delta(const Job &j, const void *stack, int x0, int y0,
                                                  int t, const float *bp, const float *basis)
 {
@@ -326,13 +357,19 @@ __global__ void __launch_bounds__(128) monitor_kernel(Job j, const void *stack,
     int sj = lo;
     int next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
     ff acc = {0.f, 0.f};
-    for (int t = t0; t < t1; t++) {
-        float d = corrected_delta(j, stack, x0, y0, t, bpl, basis);
-        ff_add(acc, d);
-        while (t + 1 == next) {
-            snap_part[(size_t)tr * j.nsnap + sj] = make_float2(acc.hi, acc.lo);
-            sj++;
-            next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
+    for (int tb = t0; tb < t1; tb += 8) {
+        float v[8];
+        window_values<8>(j, stack, x0, y0, tb, t1, v);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = tb + u;
+            if (t >= t1) break;
+            ff_add(acc, correct_value(j, v[u], t, bpl, basis));
+            while (t + 1 == next) {
+                snap_part[(size_t)tr * j.nsnap + sj] = make_float2(acc.hi, acc.lo);
+                sj++;
+                next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
+            }
         }
     }
     segtot[(size_t)tr * nseg + seg] = make_float2(acc.hi, acc.lo);
@@ -443,29 +480,33 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const void *stack,
     if (j0 == 0) u_prev = -bm.z;
     else u_prev = corrected_delta(j, stack, xa, ya, j0 - 1, bpa, basis) - bm.x;
     float segv = 0.f;
-    for (int jj = j0; jj < j1; jj++) {
-        float w;
-        if (j.is_ccf) w = corrected_delta(j, stack, xb, yb, jj, bpb, basis) - bm.y;
-        float dcur = j.is_ccf ? 0.f : corrected_delta(j, stack, xa, ya, jj, bpa, basis);
-        if (!j.is_ccf) w = dcur - bm.y;
-        float p = u_prev * w;
-        // next direct element J_{jj+1} = v_jj
-        if (j.is_ccf) u_prev = corrected_delta(j, stack, xa, ya, jj, bpa, basis) - bm.x;
-        else u_prev = dcur - bm.x;
-        int rel = jj - j0;
-        S1[0] += p;
-        S2[0] += p * p;
-        float v = p;
-        int y = 0;
-        while (y < kBlkSegLog && ((rel >> y) & 1)) {
-            v = pend[y] + v;
-            y++;
-            float m = v * (1.f / (float)(1 << y));
-            S1[y] += m;
-            S2[y] += m * m;
+    for (int tb = j0; tb < j1; tb += 8) {
+        float va[8], vb[8];
+        window_values<8>(j, stack, xa, ya, tb, j1, va);
+        if (j.is_ccf) window_values<8>(j, stack, xb, yb, tb, j1, vb);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int jj = tb + u;
+            if (jj >= j1) break;
+            float da = correct_value(j, va[u], jj, bpa, basis);
+            float w = (j.is_ccf ? correct_value(j, vb[u], jj, bpb, basis) : da) - bm.y;
+            float p = u_prev * w;
+            u_prev = da - bm.x;   // next direct element J_{jj+1} = v_jj
+            int rel = jj - j0;
+            S1[0] += p;
+            S2[0] += p * p;
+            float v = p;
+            int y = 0;
+            while (y < kBlkSegLog && ((rel >> y) & 1)) {
+                v = pend[y] + v;
+                y++;
+                float m = v * (1.f / (float)(1 << y));
+                S1[y] += m;
+                S2[y] += m * m;
+            }
+            if (y < kBlkSegLog) pend[y] = v;
+            else segv = v;
         }
-        if (y < kBlkSegLog) pend[y] = v;
-        else segv = v;
     }
     const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
     for (int y = 0; y <= kBlkSegLog; y++) { s1[o + y] = S1[y]; s2[o + y] = S2[y]; }
@@ -493,12 +534,13 @@ __global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, 
         }
     }
     for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) { S1[y] = warp_sum_d(S1[y]); S2[y] = warp_sum_d(S2[y]); }
-    if (lane != 0) return;
-    // levels above the segment: block y spans 2^(y-8) consecutive complete segments
+    // levels above the segment: block y spans 2^(y-8) consecutive complete
+    // segments; lanes take blocks, the warp reduces
     for (int y = kBlkSegLog + 1; y < blocknum; y++) {
-        int span = 1 << (y - kBlkSegLog);
-        double inv = 1.0 / (double)(1 << y);
-        for (int b = 0; (b + 1) * span <= nbseg; b++) {
+        const int span = 1 << (y - kBlkSegLog);
+        const double inv = 1.0 / (double)(1 << y);
+        double a1 = 0.0, a2 = 0.0;
+        for (int b = lane; (b + 1) * span <= nbseg; b += 32) {
             double s = 0.0;
             bool complete = true;
             for (int k = 0; k < span; k++) {
@@ -506,12 +548,15 @@ __global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, 
                 if (isnan(v)) { complete = false; break; }
                 s += (double)v;
             }
-            if (!complete) break;
+            if (!complete) continue;   // only the last block can be incomplete
             double m = s * inv;
-            S1[y] += m;
-            S2[y] += m * m;
+            a1 += m;
+            a2 += m * m;
         }
+        S1[y] = warp_sum_d(a1);
+        S2[y] = warp_sum_d(a2);
     }
+    if (lane != 0) return;
     const float4 bm = blkmon[pix];
     const double dmDm = (double)bm.z * (double)bm.w;
     const int nprod = j.num - 1;

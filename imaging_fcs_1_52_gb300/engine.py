@@ -166,6 +166,19 @@ class Plan:
         except Exception:
             pass
 
+    STAGES = ("trace+bleach", "monitors", "blocking", "correlator", "gls", "fits")
+
+    def set_timing(self, enable: bool = True):
+        check(self._L.imfcs_plan_set_timing(self._h, int(enable)), "imfcs_plan_set_timing")
+
+    def stage_times(self) -> dict:
+        """Per-stage device times (ms) of the last execution (after a sync)."""
+        ms = (C.c_float * len(self.STAGES))()
+        n = self._L.imfcs_plan_stage_times(self._h, ms, len(self.STAGES))
+        if n < 0:
+            raise _lib.ImfcsError(_lib.last_error())
+        return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}
+
     def bleach_params(self) -> np.ndarray:
         """Per-trace bleach parameters of the last execution (diagnostic)."""
         n = self.cfg.npix * (2 if (self.cfg.cfx or self.cfg.cfy) else 1)

@@ -210,6 +210,15 @@ IMFCS_API size_t imfcs_plan_scratch_bytes(const imfcs_plan *plan);
  * the number of traces. */
 IMFCS_API int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out, int max_traces);
 
+/* Stage timing (no counterpart in the reference): when enabled, every
+ * execution records CUDA events around its stages on the execution stream;
+ * imfcs_plan_stage_times() (after the stream is synchronised) returns the
+ * durations in ms of the last execution: [0] averaged trace + bleach fit,
+ * [1] monitors, [2] blocking transform, [3] correlator, [4] GLS covariance,
+ * [5] fits.  Returns the number of stages written. */
+IMFCS_API int imfcs_plan_set_timing(imfcs_plan *plan, int enable);
+IMFCS_API int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max_stages);
+
 /* Runs the whole path on a device-resident stack; outputs are device
  * pointers.  Asynchronous on `stream`. */
 IMFCS_API int imfcs_plan_execute(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,

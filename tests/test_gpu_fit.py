@@ -1,0 +1,243 @@
+"""GPU parity of the fits through the C ABI: OLS (standardFit), GLS, Bayes,
+the reference fit API (Gpufit ACF_1D / LINEAR_1D), the reference calcACF
+path, and the diffusion law -- against the FP64 oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from imaging_fcs_1_52_gb300 import _lib, engine
+from tests.helpers import ACF_TOL, FIT_TOL, acf_deviation, oracle_kwargs, run_both
+from tests.synth import brownian_stack
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bright():
+    return brownian_stack(8, 8, 6000, seed=21, density=2.0, cps=3e4)
+
+
+def fit_errors(gpu, ref, idx=(0, 1)):
+    both = (gpu["fitted"] == 1) & (ref["fitted"] == 1)
+    errs = {}
+    for i in idx:
+        errs[i] = np.abs(gpu["fitres"][both, i] - ref["fitres"][both, i]) / np.abs(ref["fitres"][both, i])
+    return both, errs
+
+
+def test_ols_fit_parity(bright):
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000, background=100)
+    gpu, ref = run_both(bright, cfg)
+    np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 48
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+    chi = np.abs(gpu["chi2"][both] - ref["chi2"][both]) / ref["chi2"][both]
+    assert chi.max() <= 1e-3
+
+
+def test_ols_fit_parity_poly_bleach_and_fit_range(bright):
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000, background=100, bleach=_lib.BLEACH_POLYNOMIAL,
+                           poly_order=4, fitstart=2, fitend=60)
+    gpu, ref = run_both(bright, cfg)
+    assert acf_deviation(gpu, ref) <= ACF_TOL
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 48
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+
+
+def test_gls_fit_parity(bright):
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000, background=100, gls=True)
+    gpu, ref = run_both(bright, cfg)
+    # GLS hands over mcov (java:9638-9642); lag 0 is 0
+    assert np.all(gpu["acf"][:, 0] == 0)
+    assert acf_deviation(gpu, ref) <= ACF_TOL
+    np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 32
+    assert np.median(errs[1]) <= FIT_TOL
+
+
+def test_bayes_probabilities(bright):
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000, background=100, bayes=True)
+    gpu, ref = run_both(bright, cfg)
+    p_g, p_r = gpu["bayes_prob"].astype(float), ref["bayes_prob"]
+    ok = np.all(np.isfinite(p_r), axis=1)
+    assert ok.sum() >= 32
+    np.testing.assert_allclose(p_g[ok].sum(1), 1.0, atol=1e-5)
+    # same model choice on every pixel where the reference is decisive
+    dec = ok & (np.abs(p_r[:, 0] - 0.5) > 0.01)
+    np.testing.assert_array_equal(p_g[dec, 0] > 0.5, p_r[dec, 0] > 0.5)
+
+
+def _acf_curves(nfits, seed=0):
+    lag, samp, mtab = oracle.lag_tables(16, 8, 50000)
+    lagtime = lag * 1e-3
+    cst = engine.model_constants()
+    rng = np.random.default_rng(seed)
+    data, var, truth = [], [], []
+    for i in range(nfits):
+        N, D = rng.uniform(2, 20), rng.uniform(0.3, 5) * 1e-12
+        par = np.array([N, D, 0, 0, 0.001, 0, 0, 0, 0, 0, 0.0])
+        g = np.array([oracle.fcs_model(par, cst, t) for t in lagtime])
+        sd = 0.01 * np.abs(g[1]) + 0.02 * np.abs(g)
+        data.append(g + rng.normal(0, 1, g.size) * sd)
+        var.append(sd ** 2)
+        truth.append(par)
+    return np.array(data), np.array(var), lagtime, cst
+
+
+def test_reference_fit_api_acf1d():
+    L = _lib.load()
+    n, npts = 40, 72
+    data, var, lagtime, cst = _acf_curves(n)
+    y = np.ascontiguousarray(data[:, 1:], np.float32)
+    w = np.ascontiguousarray(1.0 / var[:, 1:], np.float32)
+    init = np.zeros((n, 20), np.float32)
+    init[:, 0], init[:, 1] = 1.0, 1e-12
+    init[:, 11:20] = cst
+    ptf = np.zeros(20, np.int32)
+    ptf[[0, 1, 4]] = 1
+    ui = np.ascontiguousarray(lagtime[1:], np.float32)
+    outp = np.zeros((n, 20), np.float32)
+    st = np.zeros(n, np.int32)
+    chi = np.zeros(n, np.float32)
+    it = np.zeros(n, np.int32)
+    rc = L.imfcs_fit(n, npts, y.ctypes.data, w.ctypes.data, 2, init.ctypes.data, C.c_float(1e-16), 2000, 0,
+                     ptf.ctypes.data, 0, ui.nbytes, ui.ctypes.data, outp.ctypes.data, st.ctypes.data,
+                     chi.ctypes.data, it.ctypes.data)
+    assert rc == 0, _lib.last_error()
+    assert np.all(st == 0)
+    np.testing.assert_array_equal(outp[:, 11:], init[:, 11:])   # constants pass through
+    fm = np.array([1, 1, 0, 0, 1, 0, 0, 0, 0, 0, 0], np.int32)
+    for i in range(n):
+        r = oracle.fit_ols(data[i], var[i], lagtime, 1, 72, np.array([1, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0, 0.0]), fm, cst)
+        np.testing.assert_allclose(outp[i, [0, 1]], r["params"][[0, 1]], rtol=FIT_TOL)
+        # chi-square: raw weighted sum of squares, as Gpufit returns it
+        assert abs(chi[i] - r["chi2"] * (71 - 3 - 1)) <= 1e-3 * chi[i]
+
+
+def test_reference_fit_api_linear1d():
+    L = _lib.load()
+    n, npts, ncoef = 16, 1000, 5
+    rng = np.random.default_rng(3)
+    x = np.ascontiguousarray(1e-3 * (np.arange(npts) + 0.5) * 20, np.float32)
+    coefs = np.stack([rng.uniform(100, 500, n), rng.uniform(-5, -1, n), rng.uniform(0, .1, n),
+                      rng.uniform(-1e-3, 0, n), rng.uniform(0, 1e-5, n)], 1)
+    y = np.stack([np.polynomial.polynomial.polyval(x.astype(float), c) for c in coefs]) + rng.normal(0, 1, (n, npts))
+    y = np.ascontiguousarray(y, np.float32)
+    init = np.zeros((n, 11), np.float32)
+    init[:, 0] = y[:, -1]
+    ptf = np.zeros(11, np.int32)
+    ptf[:ncoef] = 1
+    outp = np.zeros((n, 11), np.float32)
+    st = np.zeros(n, np.int32)
+    rc = L.imfcs_fit(n, npts, y.ctypes.data, None, 3, init.ctypes.data, C.c_float(1e-6), 200, ncoef,
+                     ptf.ctypes.data, 0, x.nbytes, x.ctypes.data, outp.ctypes.data, st.ctypes.data, None, None)
+    assert rc == 0, _lib.last_error()
+    for i in range(n):
+        ref = np.polynomial.polynomial.polyfit(x.astype(float), y[i].astype(float), ncoef - 1)
+        f_g = np.polynomial.polynomial.polyval(x.astype(float), outp[i, :ncoef].astype(float))
+        f_r = np.polynomial.polynomial.polyval(x.astype(float), ref)
+        assert np.max(np.abs(f_g - f_r)) <= 1e-3 * np.abs(f_r).max()
+
+
+def test_reference_calc_acf_float_path():
+    """calcACF: float stack [t][h_temp][w_temp] already binned and background
+    subtracted, polynomial coefficients supplied per temp pixel."""
+    L = _lib.load()
+    raw = brownian_stack(9, 8, 4000, seed=31, density=2.0, cps=3e4)
+    bx = by = 2
+    wt, ht = 9 - bx + 1, 8 - by + 1
+    f = raw.astype(np.float64)
+    box = sum(f[:, j:j + ht, i:i + wt] for i in range(bx) for j in range(by)) - 100 * bx * by
+    pixels = np.ascontiguousarray(box, np.float32)
+    out_w, out_h, order = 3, 3, 4
+    # per temp-pixel polynomial coefficients from the oracle's own bleach fit
+    coef = np.zeros((ht, wt, order + 1))
+    for y in range(ht):
+        for x in range(wt):
+            tr, tt = oracle.intensity_trace(raw, x, y, binx=bx, biny=by, bckg=100)
+            coef[y, x], _ = oracle.poly_fit(tr, tt, order)
+    p = _lib.ACFParameters(width=out_w, height=out_h, win_star=9, hin_star=8, w_temp=wt, h_temp=ht,
+                           pixbinX=bx, pixbinY=by, binningX=bx, binningY=by, firstframe=1, lastframe=4000,
+                           framediff=4000, cfXDistance=0, cfYDistance=0, correlatorp=16, correlatorq=8,
+                           frametime=1e-3, background=100, chanum=73, isNBcalculation=0, bleachcorr_gpu=1,
+                           bleachcorr_order=order + 1, nopit=1000, ave=4)
+    acf = np.zeros((73, out_h, out_w))
+    var = np.zeros_like(acf)
+    blk = np.zeros((2, out_h, out_w))
+    samp = np.zeros(73)
+    lag = np.zeros(73, np.int32)
+    cc = np.ascontiguousarray(coef)
+    rc = L.imfcs_calc_acf(pixels.ctypes.data, acf.ctypes.data, var.ctypes.data, None, None, blk.ctypes.data,
+                          cc.ctypes.data, samp.ctypes.data, lag.ctypes.data, C.byref(p))
+    assert rc == 0, _lib.last_error()
+    lg, sp, _ = oracle.lag_tables(16, 8, 4000)
+    np.testing.assert_array_equal(lag, lg)
+    np.testing.assert_array_equal(samp, sp)
+    ref = oracle.run(raw, out_w=out_w, out_h=out_h, binx=bx, biny=by, background=100,
+                     bleach=oracle.BLEACH_POLY, poly_order=order, do_fit=False)
+    g = acf.reshape(73, -1).T
+    scale = np.abs(ref["acf"][:, 1:2])
+    assert np.max(np.abs(g[:, 1:] - ref["acf"][:, 1:]) / scale) <= ACF_TOL
+    np.testing.assert_array_equal(blk[0].ravel(), ref["blocked_ind"])
+
+
+def test_reference_binning_and_bleach_average():
+    L = _lib.load()
+    rng = np.random.default_rng(5)
+    frames, win, hin, bx, by = 100, 7, 6, 3, 2
+    x = rng.integers(0, 50, (frames, hin, win)).astype(np.float32)
+    wt, ht = win - bx + 1, hin - by + 1
+    out = np.zeros((frames, ht, wt), np.float32)
+    p = _lib.ACFParameters(win_star=win, hin_star=hin, w_temp=wt, h_temp=ht, binningX=bx, binningY=by,
+                           pixbinX=1, pixbinY=1, firstframe=1, lastframe=frames, nopit=20, ave=5)
+    assert L.imfcs_calc_binning(x.ctypes.data, out.ctypes.data, C.byref(p)) == 0
+    ref = sum(x[:, j:j + ht, i:i + wt] for i in range(bx) for j in range(by))
+    np.testing.assert_array_equal(out, ref)
+    avg = np.zeros((ht, wt, 20), np.float32)
+    assert L.imfcs_calc_data_bleach_correction(out.ctypes.data, avg.ctypes.data, C.byref(p)) == 0
+    expect = np.trunc(out.reshape(20, 5, ht, wt).sum(1) / 5).transpose(1, 2, 0)
+    np.testing.assert_array_equal(avg, expect)
+
+
+def test_diffusion_law():
+    import torch
+    L = _lib.load()
+    raw = brownian_stack(12, 12, 4000, seed=41, density=2.0, cps=3e4)
+    dev = torch.from_numpy(raw.view(np.int16)).cuda().view(torch.uint16)
+    cfg = engine.FCSConfig(width=12, height=12, frames=4000, background=100)
+    c = cfg.to_c()
+    out = np.zeros(9)
+    line = np.zeros(2)
+    rc = L.imfcs_diffusion_law(C.byref(c), C.c_void_p(dev.data_ptr()), 3, 1, 3, C.c_double(0.24e-6),
+                               C.c_double(0.4e-6), out.ctypes.data_as(C.POINTER(C.c_double)),
+                               line.ctypes.data_as(C.POINTER(C.c_double)), None)
+    assert rc == 0, _lib.last_error()
+    for u in (1, 2, 3):
+        cst = engine.model_constants(binx=u, biny=u)
+        r = oracle.run(raw, out_w=12 // u, out_h=12 // u, binx=u, biny=u, background=100,
+                       init=np.array(cfg.init), free_mask=np.array(cfg.free_mask, np.int32), cst=cst)
+        d = r["fitres"][r["fitted"] == 1, 1]
+        mean, var = d.mean() * 1e12, (d ** 2).mean() * 1e24 - (d.mean() * 1e12) ** 2
+        assert abs(out[3 * (u - 1)] - cst[6] * 1e12) <= 1e-9 * out[3 * (u - 1)]
+        assert abs(out[3 * (u - 1) + 1] - mean) <= 1e-3 * mean
+        assert abs(out[3 * (u - 1) + 2] - var) <= 1e-2 * abs(var) + 1e-6
+    x = out[0::3]
+    yv = x / out[1::3]
+    sd = x / out[1::3] ** 2 * np.sqrt(out[2::3])
+    ref, _ = oracle.line_fit(x, yv, sd)
+    np.testing.assert_allclose(line, ref, rtol=1e-6)
+
+
+def test_simulator_is_seeded_and_bleaches():
+    import torch
+    a = engine.simulate(16, 16, 3000, seed=7, tau_bleach=1.0, cps=1e5, density=2.0)
+    b = engine.simulate(16, 16, 3000, seed=7, tau_bleach=1.0, cps=1e5, density=2.0)
+    assert torch.equal(a.view(torch.int16), b.view(torch.int16))
+    m = a.view(torch.int16).float().mean(dim=(1, 2)).cpu().numpy() - 100
+    early, late = m[:300].mean(), m[-300:].mean()
+    assert late < early * np.exp(-2.4) * 1.5   # ~exp(-t/tau) emission over 3 s
