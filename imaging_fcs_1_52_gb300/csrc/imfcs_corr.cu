@@ -146,15 +146,17 @@ __device__ __forceinline__ void samples_slow(const Job &j, const CorrOut &o, con
 // block can only end on the group's last sample, y = 16m + 15).
 template <int NL, int DEL0, int PH>
 __device__ __forceinline__ void group_step(const Job &j, const CorrOut &o, const float4 *mon, int pix,
-                                           int lagbase, const float *buf0, const float *buf1, int i0,
-                                           int ybeg, int numbin, int L, int pnum, float (&w)[32],
+                                           bool valid, int lagbase, const float *buf0, const float *buf1,
+                                           int i0, int ybeg, int numbin, int L, int pnum, float (&w)[32],
                                            float *acc, float &B0, float &B1, float *head_sm)
 {
+    // every lane of the warp takes part in the vote; lanes without a pixel
+    // (last CTA) vote "fast", compute on zeros and write nothing
     const int y0 = ybeg + i0, y1 = y0 + 15;
-    const bool fast = (y0 >= 1) && (y1 < numbin) && (L >= 16);
+    const bool fast = !valid || ((y0 >= 1) && (y1 < numbin) && (L >= 16));
     if (__all_sync(0xffffffffu, fast)) {
         group16<NL, DEL0, PH>(buf0, buf1, i0, w, acc, B0, B1);
-        if ((y1 & (L - 1)) == L - 1) {
+        if (valid && (y1 & (L - 1)) == L - 1) {
             float tmp[NL];
 #pragma unroll
             for (int l = 0; l < NL; l++) tmp[l] = acc[l];
@@ -166,8 +168,9 @@ __device__ __forceinline__ void group_step(const Job &j, const CorrOut &o, const
             B1 = 0.f;
         }
     } else {
-        samples_slow<NL, DEL0>(j, o, mon, pix, lagbase, buf0, buf1, i0, i0 + 16, ybeg, numbin, L, pnum, acc,
-                               B0, B1, head_sm);
+        if (valid)
+            samples_slow<NL, DEL0>(j, o, mon, pix, lagbase, buf0, buf1, i0, i0 + 16, ybeg, numbin, L, pnum,
+                                   acc, B0, B1, head_sm);
         // keep the ring valid for the next group (positions i0+16..i0+31)
 #pragma unroll
         for (int jj = 0; jj < 16; jj++) w[(PH + 16 + jj) & 31] = buf1[(i0 + 16 + jj) * 32];
@@ -181,7 +184,7 @@ __device__ __forceinline__ void group_step(const Job &j, const CorrOut &o, const
 // multiple of 16, so groups start at y = 16m).
 template <int NL, int DEL0, bool GROUPED>
 __device__ __forceinline__ void correlate_level(const Job &j, const CorrOut &o, const float4 *mon,
-                                                int pix, int lagbase, const float *buf0,
+                                                int pix, bool valid, int lagbase, const float *buf0,
                                                 const float *buf1, int nnew, int s_begin, int numbin,
                                                 int L, int pnum, float *acc, float &B0, float &B1,
                                                 float *head_sm)
@@ -193,13 +196,13 @@ __device__ __forceinline__ void correlate_level(const Job &j, const CorrOut &o, 
 #pragma unroll
         for (int d = 0; d < kP; d++) w[d] = buf1[d * 32];
         for (int g = 0; g < nnew; g += 32) {
-            group_step<NL, DEL0, 0>(j, o, mon, pix, lagbase, buf0, buf1, g, ybeg, numbin, L, pnum, w, acc, B0, B1,
-                                    head_sm);
+            group_step<NL, DEL0, 0>(j, o, mon, pix, valid, lagbase, buf0, buf1, g, ybeg, numbin, L, pnum, w, acc,
+                                    B0, B1, head_sm);
             if (g + 16 < nnew)
-                group_step<NL, DEL0, 16>(j, o, mon, pix, lagbase, buf0, buf1, g + 16, ybeg, numbin, L, pnum, w,
-                                         acc, B0, B1, head_sm);
+                group_step<NL, DEL0, 16>(j, o, mon, pix, valid, lagbase, buf0, buf1, g + 16, ybeg, numbin, L, pnum,
+                                         w, acc, B0, B1, head_sm);
         }
-    } else {
+    } else if (valid) {
         samples_slow<NL, DEL0>(j, o, mon, pix, lagbase, buf0, buf1, 0, nnew, ybeg, numbin, L, pnum, acc, B0,
                                B1, head_sm);
     }
@@ -346,18 +349,18 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
             __syncthreads();
         }
         // level-0 samples beyond numbin are already zero (frames >= num staged as 0)
-        // ---- correlate ----
-        if (pvalid) {
+        // ---- correlate (all lanes, so that warp votes see the full warp) ----
+        {
             if (warp < 2) {
                 const int numbin0 = li_g->numbin[0];
                 const int L = 1 << ind;
                 float *hs = head0_sm + warp * (kP + 1) * 32 + lane;
                 if (warp == 0)
-                    correlate_level<9, 0, true>(j, o, mon, pix, 0, buf0 + level_off(0) + lane,
+                    correlate_level<9, 0, true>(j, o, mon, pixc, pvalid, 0, buf0 + level_off(0) + lane,
                                                 buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
                                                 pnum, acc0, B00, B10, hs);
                 else
-                    correlate_level<8, 9, true>(j, o, mon, pix, 9, buf0 + level_off(0) + lane,
+                    correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, 9, buf0 + level_off(0) + lane,
                                                 buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
                                                 pnum, acc0, B00, B10, hs);
             } else {
@@ -376,11 +379,11 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
                     const int L = 1 << (ind - k);
                     const int lagbase = (kP + 1) + (k - 1) * 8;
                     if (nk >= 16)
-                        correlate_level<8, 9, true>(j, o, mon, pix, lagbase, buf0 + level_off(k) + lane,
+                        correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
                                                     buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
                                                     B0, B1, hs);
                     else
-                        correlate_level<8, 9, false>(j, o, mon, pix, lagbase, buf0 + level_off(k) + lane,
+                        correlate_level<8, 9, false>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
                                                      buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
                                                      B0, B1, hs);
 #pragma unroll
