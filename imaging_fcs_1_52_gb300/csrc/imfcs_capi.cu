@@ -246,6 +246,7 @@ struct imfcs_plan {
     float *fit_init = nullptr, *fit_par = nullptr, *fit_chi2 = nullptr, *fit_hess = nullptr;
     int *fit_state = nullptr, *fit_iter = nullptr;
     float *lagtime = nullptr;
+    int *dev_err = nullptr;   // device-side bounded-wait failures
     double *logp1 = nullptr, *logp2 = nullptr;
     float *bfit_init1 = nullptr, *bfit_init2 = nullptr, *bfit_par = nullptr, *bfit_chi2 = nullptr,
           *bfit_hess = nullptr, *bfit_res = nullptr;
@@ -401,6 +402,7 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     AL(pl->acf_int, np * chanum);
     AL(pl->var_int, np * chanum);
     AL(pl->lagtime, chanum);
+    AL(pl->dev_err, 1);
     if (j.bleach == IMFCS_BLEACH_POLYNOMIAL) {
         AL(pl->proj, (size_t)(j.poly_order + 1) * j.nopit);
         AL(pl->basis, (size_t)(j.poly_order + 1) * j.num);
@@ -437,6 +439,7 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     }
     // constant tables
     e = cudaMemcpy(pl->li_dev, &pl->li, sizeof(LagInfo), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(pl->dev_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(pl->snap_pos, pl->li.snap_pos, sizeof(int) * kMaxSnap, cudaMemcpyHostToDevice);
     std::vector<float> lt(chanum);
     for (int x = 0; x < chanum; x++) lt[x] = (float)(pl->li.lag[x] * cfg->frametime);
@@ -575,7 +578,7 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     pl->mark(3, s);
     CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->mon, pl->blk_ind, acf, var,
                    dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats,
-                   c.gls, s));
+                   c.gls, pl->dev_err, s));
     if (dev_out->blocked_ind) CK(cudaMemcpyAsync(dev_out->blocked_ind, pl->blk_ind, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     if (dev_out->blocked_ok) CK(cudaMemcpyAsync(dev_out->blocked_ok, pl->blk_ok, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     pl->mark(4, s);
@@ -679,7 +682,10 @@ extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stac
     CK(d2h(host_out->iterations, d.iterations, np, s));
     CK(d2h(host_out->bayes_prob, d.bayes_prob, np * 2, s));
     CK(d2h(host_out->covmats, d.covmats, np * (ch - 1) * (ch - 1), s));
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, pl->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (derr) { set_error("a device-side wait timed out (TMA staging)"); return 1; }
     return 0;
 }
 

@@ -22,13 +22,17 @@
 // exactly the Java blocked product (prod after binct pairwise means).
 // Values are FP32 centred on the pixel's mean; block sums are exact-order FP32,
 // totals are float-float.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <math.h>
+#include <stdint.h>
+#include <string.h>
 
 #include "imfcs_internal.cuh"
 
 namespace imfcs {
 
-constexpr int kCorrThreads = 96;
+constexpr int kCorrThreads = 128;
 constexpr int kStatN = 5;   // per-lag block statistics: Ahi, Alo, S1, S2, r
 
 struct CorrOut {
@@ -38,6 +42,7 @@ struct CorrOut {
     int pnum_stride;
     float *stats;        // scratch [chanum][kStatN][npix]
     int gls;
+    int *err;            // set to 1 when a bounded wait gave up
 };
 
 __device__ __forceinline__ float &stat_ref(float *stats, int npix, int lag, int s, int pix)
@@ -218,41 +223,123 @@ __host__ __device__ inline int level_off(int k)
     return o;
 }
 
-// Per-level persistent state of warp 2 (levels >= 1) in shared memory:
+// Per-level persistent state of the binned-level warps in shared memory:
 // acc[8], B0, B1, head[17] per level and lane.  Level 0 keeps acc, B0, B1 in
 // registers of warps 0 and 1; each of those warps has its own head[17].
 constexpr int kLvlState = 8 + 2 + kP + 1;
 constexpr int kHead0 = 2 * (kP + 1);
 
-template <bool CCF>
-__global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo *li_g,
-                                                            const void *stack,
-                                                            const float *bparams,
-                                                            const float *basis,
-                                                            const float4 *mon, const int *blk_ind,
-                                                            CorrOut o)
+__host__ __device__ inline size_t corr_smem_floats_dev(int q, bool ccf)
 {
-    extern __shared__ float smem[];
+    return (size_t)(ccf ? 2 : 1) * level_off(q) + (size_t)q * kLvlState * 32 + kHead0 * 32;
+}
+
+// ---------------------------------------------------------------------------
+// TMA staging of the raw uint16 frames: one box [kChunk][BH][BW] per chunk,
+// loaded by one thread while the CTA correlates the previous chunk.  Waits
+// are bounded: on a timeout the CTA records an error and leaves.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_box(const CUtensorMap *tmap, void *dst, uint64_t *mbar, int x, int y,
+                                             int t, uint32_t bytes)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(t), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+// Bounded wait on an mbarrier phase.  Returns false after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(mbar);
+    for (int i = 0; i < (1 << 20); i++) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(a), "r"(parity), "r"(1000)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Window value of a trace from the staged raw tile (frame fr of the chunk).
+__device__ __forceinline__ float tile_value(const Job &j, const uint16_t *tile, int BW, int BH, int fr, int xr, int yr)
+{
+    const uint16_t *f = tile + (size_t)fr * BH * BW;
+    int acc = 0;
+    for (int k = 0; k < j.biny; k++)
+        for (int i = 0; i < j.binx; i++) acc += (int)f[(yr + k) * BW + xr + i];
+    return (float)(acc - j.background * j.binx * j.biny);
+}
+
+struct TmaGeom {
+    int use_tma;       // raw frames staged by TMA
+    int bw, bh;        // box width / height (elements); box depth is kChunk
+};
+
+template <bool CCF>
+__global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo *li_g, const void *stack,
+                                                            const float *bparams, const float *basis,
+                                                            const float4 *mon, const int *blk_ind, CorrOut o,
+                                                            TmaGeom tg, const __grid_constant__ CUtensorMap tmap)
+{
+    extern __shared__ __align__(128) float smem[];
     const int nlev = j.q;                 // levels 0..q-1
     const int buf_floats = level_off(nlev);
     float *buf0 = smem;
     float *buf1 = CCF ? smem + buf_floats : smem;
     float *lvl_state = smem + (CCF ? 2 : 1) * buf_floats;   // [level][kLvlState][32]
     float *head0_sm = lvl_state + nlev * kLvlState * 32;     // [warp 0/1][kP+1][32]
+    // [kChunk][bh][bw] raw frames (TMA destination, 128-byte aligned)
+    uint16_t *raw;
+    {
+        const uint32_t base = smem_u32(smem);
+        const uint32_t want = (base + (uint32_t)(corr_smem_floats_dev(nlev, CCF) * sizeof(float)) + 127u) & ~127u;
+        raw = (uint16_t *)((char *)smem + (want - base));
+    }
     __shared__ float sh_basis[kChunk * (kMaxPoly + 1)];
     __shared__ int sh_numbin[kMaxLevels];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ int sh_fail;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int pix = blockIdx.x * 32 + lane;
-    const bool pvalid = pix < j.npix;
-    const int pixc = pvalid ? pix : 0;
+    // CTA = a segment of 32 pixels of one output row
+    const int tiles_per_row = (j.out_w + 31) / 32;
+    const int oy = blockIdx.x / tiles_per_row, seg = blockIdx.x % tiles_per_row;
+    const int ox = seg * 32 + lane;
+    const bool pvalid = ox < j.out_w && oy < j.out_h;
+    const int pix = oy * j.out_w + ox;
+    const int pixc = pvalid ? pix : oy * j.out_w + seg * 32;
     if (tid < kMaxLevels) sh_numbin[tid] = tid < nlev ? li_g->numbin[tid] : 0;
+    if (tid == 0) sh_fail = 0;
 
     // trace origins and bleach parameters of this lane's pixel
     int xa, ya, xb, yb;
     trace_origin(j, pixc, xa, ya);
     const int trb = CCF ? j.npix + pixc : pixc;
     trace_origin(j, trb, xb, yb);
+    // tile origin (x rounded down to 8 elements for TMA alignment)
+    const int xt0 = (j.map_x0 + seg * 32) * j.pixbinx;
+    const int yt0 = (j.map_y0 + oy) * j.pixbiny;
+    const int tx0 = (min(xt0, xt0 + j.cfx)) & ~7;
+    const int ty0 = min(yt0, yt0 + j.cfy);
     float bpa[kBleachStride], bpb[kBleachStride];
 #pragma unroll
     for (int i = 0; i < kBleachStride; i++) {
@@ -267,7 +354,8 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
         int lag_lo, lag_hi;
         if (warp == 0) { lag_lo = 0; lag_hi = 9; }
         else if (warp == 1) { lag_lo = 9; lag_hi = 17; }
-        else { lag_lo = 17; lag_hi = j.chanum; }
+        else if (warp == 2) { lag_lo = 17; lag_hi = min(25, j.chanum); }
+        else { lag_lo = 25; lag_hi = j.chanum; }
         for (int lag = lag_lo; lag < lag_hi; lag++)
             for (int s = 0; s < kStatN; s++) stat_ref(o.stats, j.npix, lag, s, pix) = 0.f;
     }
@@ -278,145 +366,174 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
             buf0[level_off(k) + i] = 0.f;
             if (CCF) buf1[level_off(k) + i] = 0.f;
         }
-
-    // per-lag monitors of this warp's level-0 lags
     float acc0[9], B00 = 0.f, B10 = 0.f;
 #pragma unroll
     for (int l = 0; l < 9; l++) acc0[l] = 0.f;
     for (int i = tid; i < kHead0 * 32; i += kCorrThreads) head0_sm[i] = 0.f;
-    __syncthreads();
 
     const int order1 = j.poly_order + 1;
     const int numbin_last = li_g->numbin[nlev - 1];
-    // number of chunks: until the top level has processed all direct samples
     const int top_n = kChunk >> (nlev - 1);
     int nchunks = (numbin_last + kHist + top_n - 1) / top_n;
     const int nchunk0 = (j.num + kChunk - 1) / kChunk;
     if (nchunks < nchunk0 + 1) nchunks = nchunk0 + 1;
+    const uint32_t box_bytes = (uint32_t)kChunk * tg.bh * tg.bw * 2u;
+
+    if (tg.use_tma && tid == 0) {
+        mbar_init(&mbar, 1);
+        tma_load_box(&tmap, raw, &mbar, tx0, ty0, j.first, box_bytes);
+    }
+    // basis table of chunk 0
+    if (j.bleach == IMFCS_BLEACH_POLYNOMIAL)
+        for (int i = tid; i < kChunk * order1; i += kCorrThreads)
+            sh_basis[i] = (i / order1) < j.num ? __ldg(&basis[i]) : 0.f;
+    __syncthreads();
 
     for (int c = 0; c < nchunks; c++) {
         const int f0 = c * kChunk;
-        // ---- stage: basis table for the chunk (polynomial bleach) ----
-        if (j.bleach == IMFCS_BLEACH_POLYNOMIAL)
-            for (int i = tid; i < kChunk * order1; i += kCorrThreads) {
-                int f = f0 + i / order1;
-                sh_basis[i] = f < j.num ? __ldg(&basis[(size_t)f0 * order1 + i]) : 0.f;
-            }
-        __syncthreads();
-        // ---- stage: level 0 values ----
+        // ---- stage: level-0 values (binned, background, bleach, centred) ----
         if (f0 < j.num) {
+            if (tg.use_tma) {
+                bool ok = mbar_wait(&mbar, (uint32_t)(c & 1));
+                if (!ok) sh_fail = 1;
+            }
             for (int fr = warp; fr < kChunk; fr += kCorrThreads / 32) {
                 const int f = f0 + fr;
                 float va = 0.f, vb = 0.f;
                 if (f < j.num && pvalid) {
                     float t = (float)(j.frametime_d * (f + 1.5));
                     const float *bs = sh_basis + fr * order1;
-                    va = window_value(j, stack, xa, ya, f);
+                    va = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xa - tx0, ya - ty0)
+                                    : window_value(j, stack, xa, ya, f);
                     if (j.bleach != IMFCS_BLEACH_NONE && bpa[11] != 0.f)
                         va = bleach_correct(va, bleach_f(bpa, j.bleach, j.poly_order, t, bs), bpa[9], bpa[10]);
                     va -= bpa[12];
                     if (CCF) {
-                        vb = window_value(j, stack, xb, yb, f);
+                        vb = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xb - tx0, yb - ty0)
+                                        : window_value(j, stack, xb, yb, f);
                         if (j.bleach != IMFCS_BLEACH_NONE && bpb[11] != 0.f)
                             vb = bleach_correct(vb, bleach_f(bpb, j.bleach, j.poly_order, t, bs), bpb[9], bpb[10]);
                         vb -= bpb[12];
                     }
                 }
-                buf0[level_off(0) + (kHist + fr) * 32 + lane] = va;
-                if (CCF) buf1[level_off(0) + (kHist + fr) * 32 + lane] = vb;
+                buf0[(kHist + fr) * 32 + lane] = va;
+                if (CCF) buf1[(kHist + fr) * 32 + lane] = vb;
             }
         } else {
             for (int i = tid; i < kChunk * 32; i += kCorrThreads) {
-                buf0[level_off(0) + kHist * 32 + i] = 0.f;
-                if (CCF) buf1[level_off(0) + kHist * 32 + i] = 0.f;
+                buf0[kHist * 32 + i] = 0.f;
+                if (CCF) buf1[kHist * 32 + i] = 0.f;
             }
         }
         __syncthreads();
-        // ---- stage: levels 1..q-1 by pairwise sums (java:9467-9476) ----
-        for (int k = 1; k < nlev; k++) {
-            const int nk = kChunk >> k;
-            const int sb = c * nk;
-            for (int i = tid; i < nk * 32; i += kCorrThreads) {
-                int s = i >> 5, ln = i & 31;
-                bool v = (sb + s) < sh_numbin[k];
-                const float *p0 = buf0 + level_off(k - 1) + (kHist + 2 * s) * 32 + ln;
-                buf0[level_off(k) + (kHist + s) * 32 + ln] = v ? p0[0] + p0[32] : 0.f;
-                if (CCF) {
-                    const float *p1 = buf1 + level_off(k - 1) + (kHist + 2 * s) * 32 + ln;
-                    buf1[level_off(k) + (kHist + s) * 32 + ln] = v ? p1[0] + p1[32] : 0.f;
-                }
-            }
-            __syncthreads();
+        if (sh_fail) {
+            if (tid == 0 && o.err) atomicExch(o.err, 1);
+            return;   // uniform: every thread read sh_fail after the barrier
         }
-        // level-0 samples beyond numbin are already zero (frames >= num staged as 0)
-        // ---- correlate (all lanes, so that warp votes see the full warp) ----
-        {
-            if (warp < 2) {
-                const int numbin0 = li_g->numbin[0];
-                const int L = 1 << ind;
-                float *hs = head0_sm + warp * (kP + 1) * 32 + lane;
-                if (warp == 0)
-                    correlate_level<9, 0, true>(j, o, mon, pixc, pvalid, 0, buf0 + level_off(0) + lane,
-                                                buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
-                                                pnum, acc0, B00, B10, hs);
-                else
-                    correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, 9, buf0 + level_off(0) + lane,
-                                                buf1 + level_off(0) + lane, kChunk, c * kChunk, numbin0, L,
-                                                pnum, acc0, B00, B10, hs);
-            } else {
+        // the raw tile is free again: prefetch the next chunk's frames
+        if (tg.use_tma && tid == 0 && f0 + kChunk < j.num)
+            tma_load_box(&tmap, raw, &mbar, tx0, ty0, j.first + f0 + kChunk, box_bytes);
+
+        // ---- correlate (all lanes take part, so warp votes see full warps) ----
+        const int numbin0 = sh_numbin[0];
+        if (warp < 2) {
+            const int L = 1 << ind;
+            float *hs = head0_sm + warp * (kP + 1) * 32 + lane;
+            if (warp == 0)
+                correlate_level<9, 0, true>(j, o, mon, pixc, pvalid, 0, buf0 + lane, buf1 + lane, kChunk, f0,
+                                            numbin0, L, pnum, acc0, B00, B10, hs);
+            else
+                correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, 9, buf0 + lane, buf1 + lane, kChunk, f0,
+                                            numbin0, L, pnum, acc0, B00, B10, hs);
+        } else {
+            if (warp == 2) {
+                // build the binned levels 1..q-1 by pairwise sums (java:9467-9476)
                 for (int k = 1; k < nlev; k++) {
-                    const int nk = kChunk >> k;
-                    const int numbin = li_g->numbin[k];
-                    const int sb = c * nk;
-                    if (sb - kHist >= numbin) continue;
-                    float *st = lvl_state + (size_t)k * kLvlState * 32;
-                    float acc[8], B0, B1;
-#pragma unroll
-                    for (int l = 0; l < 8; l++) acc[l] = st[l * 32 + lane];
-                    B0 = st[8 * 32 + lane];
-                    B1 = st[9 * 32 + lane];
-                    float *hs = st + 10 * 32 + lane;
-                    const int L = 1 << (ind - k);
-                    const int lagbase = (kP + 1) + (k - 1) * 8;
-                    if (nk >= 16)
-                        correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
-                                                    buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
-                                                    B0, B1, hs);
-                    else
-                        correlate_level<8, 9, false>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
-                                                     buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc,
-                                                     B0, B1, hs);
-#pragma unroll
-                    for (int l = 0; l < 8; l++) st[l * 32 + lane] = acc[l];
-                    st[8 * 32 + lane] = B0;
-                    st[9 * 32 + lane] = B1;
+                    const int nk = kChunk >> k, sb = c * nk, nb = sh_numbin[k];
+                    for (int s = 0; s < nk; s++) {
+                        const bool v = (sb + s) < nb;
+                        const float *p0 = buf0 + level_off(k - 1) + (kHist + 2 * s) * 32 + lane;
+                        buf0[level_off(k) + (kHist + s) * 32 + lane] = v ? p0[0] + p0[32] : 0.f;
+                        if (CCF) {
+                            const float *p1 = buf1 + level_off(k - 1) + (kHist + 2 * s) * 32 + lane;
+                            buf1[level_off(k) + (kHist + s) * 32 + lane] = v ? p1[0] + p1[32] : 0.f;
+                        }
+                    }
+                    __syncwarp();
                 }
+                asm volatile("bar.arrive 1, 64;" ::: "memory");
+            } else {
+                asm volatile("bar.sync 1, 64;" ::: "memory");
+            }
+            // warp 2: level 1; warp 3: levels 2..q-1
+            const int kb = (warp == 2) ? 1 : 2, ke = (warp == 2) ? min(2, nlev) : nlev;
+            for (int k = kb; k < ke; k++) {
+                const int nk = kChunk >> k;
+                const int numbin = sh_numbin[k];
+                const int sb = c * nk;
+                if (sb - kHist >= numbin) continue;
+                float *st = lvl_state + (size_t)k * kLvlState * 32;
+                float acc[8], B0, B1;
+#pragma unroll
+                for (int l = 0; l < 8; l++) acc[l] = st[l * 32 + lane];
+                B0 = st[8 * 32 + lane];
+                B1 = st[9 * 32 + lane];
+                float *hs = st + 10 * 32 + lane;
+                const int L = 1 << (ind - k);
+                const int lagbase = (kP + 1) + (k - 1) * 8;
+                if (nk >= 16)
+                    correlate_level<8, 9, true>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
+                                                buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc, B0, B1, hs);
+                else
+                    correlate_level<8, 9, false>(j, o, mon, pixc, pvalid, lagbase, buf0 + level_off(k) + lane,
+                                                 buf1 + level_off(k) + lane, nk, sb, numbin, L, pnum, acc, B0, B1, hs);
+#pragma unroll
+                for (int l = 0; l < 8; l++) st[l * 32 + lane] = acc[l];
+                st[8 * 32 + lane] = B0;
+                st[9 * 32 + lane] = B1;
             }
         }
         __syncthreads();
-        // ---- shift history: last kHist samples of each level to the front ----
-        // (source and destination overlap for levels with fewer than kHist
-        // new samples, so read everything first, then write)
-        constexpr int kPer = (kHist * 32 + kCorrThreads - 1) / kCorrThreads;
+        // ---- shift history: the last kHist samples of each level to the
+        // front.  Levels with at least kHist new samples copy in place (no
+        // overlap); the others (at most 4: kChunk/2^k < kHist) overlap source
+        // and destination and go through registers.
+        float hv0[4][4], hv1[4][4];
         for (int k = 0; k < nlev; k++) {
             const int nk = kChunk >> k;
-            float v0[kPer], v1[kPer];
-#pragma unroll
-            for (int r = 0; r < kPer; r++) {
-                int i = tid + r * kCorrThreads;
-                v0[r] = i < kHist * 32 ? buf0[level_off(k) + nk * 32 + i] : 0.f;
-                v1[r] = (CCF && i < kHist * 32) ? buf1[level_off(k) + nk * 32 + i] : 0.f;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < kPer; r++) {
-                int i = tid + r * kCorrThreads;
-                if (i < kHist * 32) {
-                    buf0[level_off(k) + i] = v0[r];
-                    if (CCF) buf1[level_off(k) + i] = v1[r];
+            if (nk >= kHist) {
+                for (int i = tid; i < kHist * 32; i += kCorrThreads) {
+                    buf0[level_off(k) + i] = buf0[level_off(k) + nk * 32 + i];
+                    if (CCF) buf1[level_off(k) + i] = buf1[level_off(k) + nk * 32 + i];
                 }
             }
         }
+        const int ksmall = 5;   // kChunk >> k < kHist for k >= 4 (kChunk = 128, kHist = 16)
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int k = ksmall - 1 + m;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int i = tid + r * kCorrThreads;
+                hv0[m][r] = (k < nlev) ? buf0[level_off(k) + (kChunk >> k) * 32 + i] : 0.f;
+                hv1[m][r] = (CCF && k < nlev) ? buf1[level_off(k) + (kChunk >> k) * 32 + i] : 0.f;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const int k = ksmall - 1 + m;
+            if (k >= nlev) continue;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int i = tid + r * kCorrThreads;
+                buf0[level_off(k) + i] = hv0[m][r];
+                if (CCF) buf1[level_off(k) + i] = hv1[m][r];
+            }
+        }
+        if (j.bleach == IMFCS_BLEACH_POLYNOMIAL && f0 + kChunk < j.num)
+            for (int i = tid; i < kChunk * order1; i += kCorrThreads)
+                sh_basis[i] = (f0 + kChunk + i / order1) < j.num ? __ldg(&basis[(size_t)(f0 + kChunk) * order1 + i]) : 0.f;
         __syncthreads();
     }
 
@@ -425,7 +542,8 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
     int lag_lo, lag_hi;
     if (warp == 0) lag_lo = 0, lag_hi = 9;
     else if (warp == 1) lag_lo = 9, lag_hi = 17;
-    else lag_lo = 17, lag_hi = j.chanum;
+    else if (warp == 2) lag_lo = 17, lag_hi = min(25, j.chanum);
+    else lag_lo = 25, lag_hi = j.chanum;
     for (int lag = lag_lo; lag < lag_hi; lag++) {
         float rem;
         if (warp < 2) {
@@ -466,33 +584,82 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
     }
 }
 
-template __global__ void corr_kernel<false>(Job, const LagInfo *, const void *, const float *,
-                                            const float *, const float4 *, const int *, CorrOut);
-template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, const float *,
-                                           const float *, const float4 *, const int *, CorrOut);
+template __global__ void corr_kernel<false>(Job, const LagInfo *, const void *, const float *, const float *,
+                                            const float4 *, const int *, CorrOut, TmaGeom,
+                                            const __grid_constant__ CUtensorMap);
+template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, const float *, const float *,
+                                           const float4 *, const int *, CorrOut, TmaGeom,
+                                           const __grid_constant__ CUtensorMap);
 
-// Host-visible launch helper.
-size_t corr_smem_bytes(int q, bool ccf)
+// ---------------------------------------------------------------------------
+// Host side: shared memory size, TMA geometry and tensor map, launch.
+// ---------------------------------------------------------------------------
+size_t corr_smem_bytes(int q, bool ccf) { return corr_smem_floats_dev(q, ccf) * sizeof(float); }
+
+// TMA box over the raw stack that covers every window of a 32-pixel row
+// segment (x rounded down to 8 elements = 16 bytes).
+static TmaGeom tma_geometry(const Job &j, const void *stack)
 {
-    return (size_t)((ccf ? 2 : 1) * level_off(q) + q * kLvlState * 32 + kHead0 * 32) * sizeof(float);
+    TmaGeom g{0, 0, 0};
+    if (j.input_float) return g;
+    if ((j.in_w % 8) != 0 || ((uintptr_t)stack % 16) != 0) return g;
+    int bw = 31 * j.pixbinx + j.binx + abs(j.cfx) + 7;
+    bw = (bw + 7) & ~7;
+    int bh = j.biny + abs(j.cfy);
+    if (bw > 256 || bh > 256) return g;
+    size_t bytes = (size_t)kChunk * bw * bh * 2;
+    if (bytes > 40 * 1024) return g;
+    g.use_tma = 1;
+    g.bw = bw;
+    g.bh = bh;
+    return g;
+}
+
+static bool encode_stack_map(const Job &j, const void *stack, const TmaGeom &g, CUtensorMap *map)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return false;
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    const int frames_total = j.first + j.num;
+    cuuint64_t dims[3] = {(cuuint64_t)j.in_w, (cuuint64_t)j.in_h, (cuuint64_t)frames_total};
+    cuuint64_t strides[2] = {(cuuint64_t)j.in_w * 2, (cuuint64_t)j.in_w * j.in_h * 2};
+    cuuint32_t box[3] = {(cuuint32_t)g.bw, (cuuint32_t)g.bh, (cuuint32_t)kChunk};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(stack), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
 }
 
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
                         const float *basis, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
-                        int pnum_stride, float *stats, int gls, cudaStream_t stream)
+                        int pnum_stride, float *stats, int gls, int *err, cudaStream_t stream)
 {
     CorrOut o;
     o.acf = acf; o.var = var; o.sd = sd; o.nb_mean = nb_mean; o.nb_cov = nb_cov;
-    o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls;
+    o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls; o.err = err;
+    TmaGeom g = tma_geometry(j, stack);
+    CUtensorMap map;
+    memset(&map, 0, sizeof(map));
+    if (g.use_tma && !encode_stack_map(j, stack, g, &map)) g.use_tma = 0;
     size_t smem = corr_smem_bytes(j.q, j.is_ccf);
-    dim3 grid((j.npix + 31) / 32);
+    if (g.use_tma) smem += 128 + (size_t)kChunk * g.bw * g.bh * 2;   // 128: alignment slack
+    const int tiles_per_row = (j.out_w + 31) / 32;
+    dim3 grid(tiles_per_row * j.out_h);
     if (j.is_ccf) {
         cudaFuncSetAttribute(corr_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        corr_kernel<true><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o);
+        corr_kernel<true><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o, g, map);
     } else {
         cudaFuncSetAttribute(corr_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        corr_kernel<false><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o);
+        corr_kernel<false><<<grid, kCorrThreads, smem, stream>>>(j, li, stack, bparams, basis, mon, blk_ind, o, g, map);
     }
     return cudaGetLastError();
 }

@@ -26,9 +26,9 @@ constexpr int kPtsPerLane = kMaxPts / 32;
 
 template <int KM>
 struct LMState {
-    float A[KM * KM];
-    float g[KM];
-    float chi2;
+    double A[KM * KM];
+    double g[KM];
+    double chi2;
 };
 
 __device__ __forceinline__ ModelConst load_consts(const float *c)
@@ -43,10 +43,20 @@ __device__ __forceinline__ ModelConst load_consts(const float *c)
     return m;
 }
 
-// Evaluate model value and the gradient w.r.t. the free parameters at x.
+__device__ __forceinline__ ModelConstD to_double(const ModelConst &m)
+{
+    ModelConstD d;
+    d.ax = m.ax; d.ay = m.ay; d.s = m.s; d.sz = m.sz; d.rx = m.rx; d.ry = m.ry;
+    d.inv_norm = m.inv_norm; d.q2 = m.q2; d.q3 = m.q3;
+    return d;
+}
+
+// Model value and gradient w.r.t. the free parameters at x.  precise: the
+// value comes from the FP64 model (ACF model); the gradient is always FP32.
 template <int KM>
-__device__ __forceinline__ float model_eval(const FitArgs &a, const ModelConst &mc, const float *par,
-                                            float x, float *gfree, bool c2, bool c3)
+__device__ __forceinline__ double model_eval(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd,
+                                             const float *par, const double *pard, float x, float *gfree,
+                                             bool c2, bool c3, bool precise)
 {
     if (a.model == IMFCS_MODEL_ACF_1D) {
         float g[IMFCS_NPARAM];
@@ -54,10 +64,11 @@ __device__ __forceinline__ float model_eval(const FitArgs &a, const ModelConst &
 #pragma unroll
         for (int i = 0; i < KM; i++)
             if (i < a.k) gfree[i] = g[a.idx[i]];
-        return v;
+        return precise ? fcs_model_value_d(pard, mcd, (double)x, c2, c3) : (double)v;
     } else {
-        float v = 0.f, pw = 1.f, g[IMFCS_NPARAM];
-        for (int i = 0; i < a.np; i++) { g[i] = pw; v = fmaf(par[i], pw, v); pw *= x; }
+        float g[IMFCS_NPARAM];
+        double v = 0.0, pw = 1.0;
+        for (int i = 0; i < a.np; i++) { g[i] = (float)pw; v = fma(pard[i], pw, v); pw *= (double)x; }
 #pragma unroll
         for (int i = 0; i < KM; i++)
             if (i < a.k) gfree[i] = g[a.idx[i]];
@@ -66,15 +77,19 @@ __device__ __forceinline__ float model_eval(const FitArgs &a, const ModelConst &
 }
 
 // One evaluation: chi^2, A = J^T W J, g = J^T W r over all points (warp).
-// For GLS the model vector and Jacobian are first transformed by L^-1 held in
-// shared memory (packed lower triangle), with the transformed data in y.
+// Per-lane partial sums in FP32 (a handful of points each), warp reduction in
+// FP64; chi^2 and the residuals in FP64.  For GLS the model vector and the
+// Jacobian are first transformed by L^-1 held in shared memory (packed lower
+// triangle); y then holds the transformed data.
 template <int KM>
-__device__ void evaluate(const FitArgs &a, const ModelConst &mc, const float *par, const float *yl,
-                         const float *wl, const float *xl, int lane, float *sh_fj,
-                         const float *sh_linv, LMState<KM> &s, bool c2, bool c3)
+__device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd, const float *par,
+                         const double *pard, const float *yl, const float *wl, const float *xl, int lane,
+                         float *sh_fj, double *sh_f64, const float *sh_linv, LMState<KM> &s, bool c2,
+                         bool c3, bool precise)
 {
-    constexpr int NACC = KM * (KM + 1) / 2 + KM + 1;
+    constexpr int NACC = KM * (KM + 1) / 2 + KM;
     float acc[NACC];
+    double c2acc = 0.0;
 #pragma unroll
     for (int i = 0; i < NACC; i++) acc[i] = 0.f;
     const int n = a.npts;
@@ -84,8 +99,9 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const float *pa
             int i = lane + 32 * m;
             if (i < n) {
                 float gr[KM];
-                float f = model_eval<KM>(a, mc, par, xl[m], gr, c2, c3);
-                float r = yl[m] - f, w = wl[m];
+                double f = model_eval<KM>(a, mc, mcd, par, pard, xl[m], gr, c2, c3, precise);
+                double rd = (double)yl[m] - f;
+                float r = (float)rd, w = wl[m];
                 int q = 0;
 #pragma unroll
                 for (int p = 0; p < KM; p++)
@@ -93,20 +109,19 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const float *pa
                     for (int t = 0; t <= p; t++) acc[q++] += w * gr[p] * gr[t];
 #pragma unroll
                 for (int p = 0; p < KM; p++) acc[q++] += w * gr[p] * r;
-                acc[q] += w * r * r;
+                c2acc += (double)w * rd * rd;
             }
         }
     } else {
-        // model and Jacobian into shared memory: sh_fj[(1+KM) * n]
 #pragma unroll
         for (int m = 0; m < kPtsPerLane; m++) {
             int i = lane + 32 * m;
             if (i < n) {
                 float gr[KM];
-                float f = model_eval<KM>(a, mc, par, xl[m], gr, c2, c3);
-                sh_fj[i] = f;
+                double f = model_eval<KM>(a, mc, mcd, par, pard, xl[m], gr, c2, c3, precise);
+                sh_f64[i] = f;
 #pragma unroll
-                for (int p = 0; p < KM; p++) sh_fj[(1 + p) * n + i] = (p < a.k) ? gr[p] : 0.f;
+                for (int p = 0; p < KM; p++) sh_fj[p * n + i] = (p < a.k) ? gr[p] : 0.f;
             }
         }
         __syncwarp();
@@ -115,16 +130,18 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const float *pa
             int i = lane + 32 * m;
             if (i < n) {
                 const float *row = sh_linv + (size_t)i * (i + 1) / 2;
-                float f = 0.f, gr[KM];
+                double f = 0.0;
+                float gr[KM];
 #pragma unroll
                 for (int p = 0; p < KM; p++) gr[p] = 0.f;
                 for (int c = 0; c <= i; c++) {
                     float l = row[c];
-                    f = fmaf(l, sh_fj[c], f);
+                    f = fma((double)l, sh_f64[c], f);
 #pragma unroll
-                    for (int p = 0; p < KM; p++) gr[p] = fmaf(l, sh_fj[(1 + p) * n + c], gr[p]);
+                    for (int p = 0; p < KM; p++) gr[p] = fmaf(l, sh_fj[p * n + c], gr[p]);
                 }
-                float r = yl[m] - f;
+                double rd = (double)yl[m] - f;
+                float r = (float)rd;
                 int q = 0;
 #pragma unroll
                 for (int p = 0; p < KM; p++)
@@ -132,28 +149,30 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const float *pa
                     for (int t = 0; t <= p; t++) acc[q++] += gr[p] * gr[t];
 #pragma unroll
                 for (int p = 0; p < KM; p++) acc[q++] += gr[p] * r;
-                acc[q] += r * r;
+                c2acc += rd * rd;
             }
         }
         __syncwarp();
     }
-#pragma unroll
-    for (int i = 0; i < NACC; i++) acc[i] = warp_sum(acc[i]);
     int q = 0;
 #pragma unroll
     for (int p = 0; p < KM; p++)
 #pragma unroll
-        for (int t = 0; t <= p; t++) { s.A[p * KM + t] = acc[q]; s.A[t * KM + p] = acc[q]; q++; }
+        for (int t = 0; t <= p; t++) {
+            double v = warp_sum_d((double)acc[q++]);
+            s.A[p * KM + t] = v;
+            s.A[t * KM + p] = v;
+        }
 #pragma unroll
-    for (int p = 0; p < KM; p++) s.g[p] = acc[q++];
-    s.chi2 = acc[q];
+    for (int p = 0; p < KM; p++) s.g[p] = warp_sum_d((double)acc[q++]);
+    s.chi2 = warp_sum_d(c2acc);
 }
 
 template <int KM>
-__device__ __forceinline__ bool chol_solve_f(const float *Ain, const float *b, int k, float lambda,
-                                             const float *dscale, float *x)
+__device__ __forceinline__ bool chol_solve_d(const double *Ain, const double *b, int k, double lambda,
+                                             const double *dscale, double *x)
 {
-    float L[KM * KM];
+    double L[KM * KM];
 #pragma unroll
     for (int i = 0; i < KM * KM; i++) L[i] = Ain[i];
 #pragma unroll
@@ -162,29 +181,29 @@ __device__ __forceinline__ bool chol_solve_f(const float *Ain, const float *b, i
 #pragma unroll
     for (int c = 0; c < KM; c++) {
         if (c >= k) break;
-        float d = L[c * KM + c];
+        double d = L[c * KM + c];
 #pragma unroll
         for (int m = 0; m < KM; m++)
             if (m < c) d -= L[c * KM + m] * L[c * KM + m];
-        if (!(d > 0.f) || !isfinite(d)) return false;
-        d = sqrtf(d);
+        if (!(d > 0.0) || !isfinite(d)) return false;
+        d = sqrt(d);
         L[c * KM + c] = d;
-        float id = 1.f / d;
+        double id = 1.0 / d;
 #pragma unroll
         for (int r = 0; r < KM; r++) {
             if (r <= c || r >= k) continue;
-            float sum = L[r * KM + c];
+            double sum = L[r * KM + c];
 #pragma unroll
             for (int m = 0; m < KM; m++)
                 if (m < c) sum -= L[r * KM + m] * L[c * KM + m];
             L[r * KM + c] = sum * id;
         }
     }
-    float yv[KM];
+    double yv[KM];
 #pragma unroll
     for (int r = 0; r < KM; r++) {
-        if (r >= k) { yv[r] = 0.f; continue; }
-        float sum = b[r];
+        if (r >= k) { yv[r] = 0.0; continue; }
+        double sum = b[r];
 #pragma unroll
         for (int m = 0; m < KM; m++)
             if (m < r) sum -= L[r * KM + m] * yv[m];
@@ -192,8 +211,8 @@ __device__ __forceinline__ bool chol_solve_f(const float *Ain, const float *b, i
     }
 #pragma unroll
     for (int r = KM - 1; r >= 0; r--) {
-        if (r >= k) { x[r] = 0.f; continue; }
-        float sum = yv[r];
+        if (r >= k) { x[r] = 0.0; continue; }
+        double sum = yv[r];
 #pragma unroll
         for (int m = 0; m < KM; m++)
             if (m > r && m < k) sum -= L[m * KM + r] * x[m];
@@ -210,8 +229,15 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
     const int wpb = blockDim.x >> 5;
     const int n = a.npts;
     const int linv_len = n * (n + 1) / 2;
-    float *sh_linv = a.linv ? fsh + (size_t)wib * (linv_len + (1 + KM) * n) : nullptr;
+    // per warp (GLS only): L^-1 (float), Jacobian (float), model values (double)
+    const size_t per_warp = (size_t)linv_len + KM * n + 2 * n + 2;
+    float *sh_linv = a.linv ? fsh + (size_t)wib * per_warp : nullptr;
     float *sh_fj = a.linv ? sh_linv + linv_len : nullptr;
+    double *sh_f64 = nullptr;
+    if (a.linv) {
+        size_t off = ((size_t)(sh_fj + KM * n - fsh) + 1) & ~(size_t)1;   // 8-byte aligned
+        sh_f64 = (double *)(fsh + off);
+    }
     const int gw = blockIdx.x * wpb + wib, nw = gridDim.x * wpb;
 
     float xl[kPtsPerLane];
@@ -234,101 +260,121 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
             for (int i = lane; i < linv_len; i += 32) sh_linv[i] = __ldg(&src[i]);
             __syncwarp();
         }
-        ModelConst mc = a.cst ? load_consts(a.cst + (size_t)fit * IMFCS_NCONST) : a.mc;
+        const ModelConst mc = a.cst ? load_consts(a.cst + (size_t)fit * IMFCS_NCONST) : a.mc;
+        const ModelConstD mcd = to_double(mc);
         float par[IMFCS_NPARAM];
+        double pard[IMFCS_NPARAM];
         const float *ip = a.init + (size_t)fit * a.init_stride;
-        for (int i = 0; i < a.np; i++) par[i] = __ldg(&ip[i]);
+        for (int i = 0; i < a.np; i++) { par[i] = __ldg(&ip[i]); pard[i] = par[i]; }
         bool c2 = false, c3 = false;
         if (a.model == IMFCS_MODEL_ACF_1D) {
             bool f2free = false, f3free = false;
-            for (int i = 0; i < a.k; i++) { f2free |= (a.idx[i] == 5 || a.idx[i] == 6); f3free |= (a.idx[i] == 7 || a.idx[i] == 8); }
+            for (int i = 0; i < a.k; i++) {
+                f2free |= (a.idx[i] == 5 || a.idx[i] == 6);
+                f3free |= (a.idx[i] == 7 || a.idx[i] == 8);
+            }
             c2 = par[5] != 0.f || f2free;
             c3 = par[7] != 0.f || f3free;
         }
+        // Gpufit mode (tol > 0): FP32 model values throughout.  Step mode:
+        // FP32 values until the Gauss-Newton step is small, then a polish with
+        // FP64 model values.
+        bool precise = (a.model != IMFCS_MODEL_ACF_1D);
+        int polish = 0;
         LMState<KM> s;
-        evaluate<KM>(a, mc, par, yl, wl, xl, lane, sh_fj, sh_linv, s, c2, c3);
+        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, precise);
         int state = IMFCS_STATE_MAX_ITERATIONS, it = 0;
-        float lambda = 1e-3f;
-        float dscale[KM];
+        double lambda = 1e-3;
+        double dscale[KM];
 #pragma unroll
-        for (int i = 0; i < KM; i++) dscale[i] = (i < a.k) ? fmaxf(s.A[i * KM + i], 1e-30f) : 1.f;
+        for (int i = 0; i < KM; i++) dscale[i] = (i < a.k) ? fmax(s.A[i * KM + i], 1e-300) : 1.0;
         if (!isfinite(s.chi2)) state = IMFCS_STATE_SINGULAR_HESSIAN;
         else if (a.k == 0) state = IMFCS_STATE_CONVERGED;
         for (it = 0; state == IMFCS_STATE_MAX_ITERATIONS && it < a.max_iter; it++) {
-            float h[KM];
+            double h[KM];
             if (a.tol <= 0.f) {
-                // converged when the undamped Gauss-Newton step is negligible:
-                // |h_i| <= 1e-6 |p_i| + 1e-5 sigma_i (sigma_i = 1/sqrt(A_ii))
-                float hg[KM], zero[KM];
+                // convergence on the undamped Gauss-Newton step
+                double hg[KM], zero[KM];
 #pragma unroll
-                for (int i = 0; i < KM; i++) zero[i] = 0.f;
-                if (chol_solve_f<KM>(s.A, s.g, a.k, 0.f, zero, hg)) {
+                for (int i = 0; i < KM; i++) zero[i] = 0.0;
+                if (chol_solve_d<KM>(s.A, s.g, a.k, 0.0, zero, hg)) {
+                    const double rel = precise ? 1e-9 : 1e-6, sg = precise ? 1e-7 : 1e-5;
                     bool conv = true;
 #pragma unroll
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) {
-                            float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
-                            conv = conv && (fabsf(hg[i]) <= 1e-6f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
+                            double sig = 1.0 / sqrt(fmax(s.A[i * KM + i], 1e-300));
+                            conv = conv && (fabs(hg[i]) <= rel * fabs(pard[a.idx[i]]) + sg * sig);
                         }
-                    if (conv) { state = IMFCS_STATE_CONVERGED; break; }
+                    if (conv || polish >= 8) {
+                        if (precise) { state = IMFCS_STATE_CONVERGED; break; }
+                        precise = true;   // switch to FP64 residuals and polish
+                        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
+                                     true);
+                        lambda = 1e-9;
+                        continue;
+                    }
                 }
+                if (precise) polish++;
             }
-            if (!chol_solve_f<KM>(s.A, s.g, a.k, lambda, dscale, h)) {
-                lambda *= 10.f;
-                if (lambda > 1e15f) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
+            if (!chol_solve_d<KM>(s.A, s.g, a.k, lambda, dscale, h)) {
+                lambda *= 10.0;
+                if (lambda > 1e15) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
                 continue;
             }
-            float pn[IMFCS_NPARAM];
-            for (int i = 0; i < a.np; i++) pn[i] = par[i];
-            bool small = true;
+            double pnd[IMFCS_NPARAM];
+            float pnf[IMFCS_NPARAM];
+            for (int i = 0; i < a.np; i++) pnd[i] = pard[i];
 #pragma unroll
             for (int i = 0; i < KM; i++)
-                if (i < a.k) {
-                    int pi = a.idx[i];
-                    pn[pi] = par[pi] + h[i];
-                    float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
-                    small = small && (fabsf(h[i]) <= 1e-6f * fabsf(par[pi]) + 1e-4f * sig);
-                }
+                if (i < a.k) pnd[a.idx[i]] = pard[a.idx[i]] + h[i];
+            for (int i = 0; i < a.np; i++) pnf[i] = (float)pnd[i];
             LMState<KM> sn;
-            evaluate<KM>(a, mc, pn, yl, wl, xl, lane, sh_fj, sh_linv, sn, c2, c3);
+            evaluate<KM>(a, mc, mcd, pnf, pnd, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, sn, c2, c3, precise);
             bool finite = isfinite(sn.chi2);
             if (a.tol > 0.f) {
                 // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487)
-                bool found = finite && fabsf(sn.chi2 - s.chi2) < a.tol * fmaxf(1.f, sn.chi2);
+                bool found = finite && fabs(sn.chi2 - s.chi2) < (double)a.tol * fmax(1.0, sn.chi2);
                 if (finite && sn.chi2 < s.chi2) {
-                    for (int i = 0; i < a.np; i++) par[i] = pn[i];
+                    for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
                     s = sn;
-                    lambda *= 0.1f;
+                    lambda *= 0.1;
                 } else {
-                    lambda *= 10.f;
+                    lambda *= 10.0;
                 }
 #pragma unroll
                 for (int i = 0; i < KM; i++)
-                    if (i < a.k) dscale[i] = fmaxf(dscale[i], s.A[i * KM + i]);
+                    if (i < a.k) dscale[i] = fmax(dscale[i], s.A[i * KM + i]);
                 if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                if (lambda > 1e30) { state = IMFCS_STATE_CONVERGED; it++; break; }
             } else {
                 if (finite && sn.chi2 < s.chi2) {
-                    for (int i = 0; i < a.np; i++) par[i] = pn[i];
+                    for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
                     s = sn;
-                    lambda = fmaxf(lambda * 0.1f, 1e-9f);
+                    lambda = fmax(lambda * 0.1, 1e-9);
 #pragma unroll
                     for (int i = 0; i < KM; i++)
-                        if (i < a.k) dscale[i] = fmaxf(dscale[i], s.A[i * KM + i]);
-                    (void)small;
+                        if (i < a.k) dscale[i] = fmax(dscale[i], s.A[i * KM + i]);
                 } else {
-                    lambda *= 10.f;
-                    if (lambda > 1e12f) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                    lambda *= 10.0;
+                    if (lambda > 1e12) {
+                        if (precise) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                        precise = true;
+                        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
+                                     true);
+                        lambda = 1e-9;
+                    }
                 }
             }
         }
         if (lane == 0) {
-            for (int i = 0; i < a.np; i++) a.out_par[(size_t)fit * a.out_stride + i] = par[i];
-            if (a.out_chi2) a.out_chi2[fit] = s.chi2;
+            for (int i = 0; i < a.np; i++) a.out_par[(size_t)fit * a.out_stride + i] = (float)pard[i];
+            if (a.out_chi2) a.out_chi2[fit] = (float)s.chi2;
             if (a.out_state) a.out_state[fit] = state;
             if (a.out_iter) a.out_iter[fit] = it;
             if (a.out_hess)
-                for (int i = 0; i < a.k * a.k; i++) a.out_hess[(size_t)fit * a.k * a.k + i] = s.A[(i / a.k) * KM + (i % a.k)];
+                for (int i = 0; i < a.k * a.k; i++)
+                    a.out_hess[(size_t)fit * a.k * a.k + i] = (float)s.A[(i / a.k) * KM + (i % a.k)];
         }
         __syncwarp();
     }
@@ -341,7 +387,7 @@ template __global__ void lm_kernel<11>(FitArgs);
 size_t lm_smem_bytes(const FitArgs &a, int km, int warps)
 {
     if (!a.linv) return 0;
-    return (size_t)warps * (a.npts * (a.npts + 1) / 2 + (1 + km) * a.npts) * sizeof(float);
+    return (size_t)warps * ((size_t)a.npts * (a.npts + 1) / 2 + km * a.npts + 2 * a.npts + 2) * sizeof(float);
 }
 
 cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream)

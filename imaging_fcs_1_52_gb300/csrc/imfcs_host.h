@@ -12,7 +12,7 @@ namespace imfcs {
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
                         const float *basis, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
-                        int pnum_stride, float *stats, int gls, cudaStream_t stream);
+                        int pnum_stride, float *stats, int gls, int *err, cudaStream_t stream);
 size_t corr_smem_bytes(int q, bool ccf);
 
 struct FitArgs;

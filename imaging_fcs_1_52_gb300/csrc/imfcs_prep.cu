@@ -142,33 +142,70 @@ __device__ __forceinline__ void exp_eval(const float *p, float t, float &f, floa
 }
 
 template <int K>
-__device__ bool solve_spd(float *a, const float *b, float *x)
+__device__ bool solve_spd(double *a, const double *b, double *x)
 {
-    // in-place Cholesky (lower) of a (K x K) then solve
+    // in-place Cholesky (lower) of a (K x K) then solve, FP64
     for (int c = 0; c < K; c++) {
-        float d = a[c * K + c];
+        double d = a[c * K + c];
         for (int m = 0; m < c; m++) d -= a[c * K + m] * a[c * K + m];
-        if (!(d > 0.f)) return false;
-        d = sqrtf(d);
+        if (!(d > 0.0)) return false;
+        d = sqrt(d);
         a[c * K + c] = d;
         for (int r = c + 1; r < K; r++) {
-            float s = a[r * K + c];
+            double s = a[r * K + c];
             for (int m = 0; m < c; m++) s -= a[r * K + m] * a[c * K + m];
             a[r * K + c] = s / d;
         }
     }
-    float yv[K];
+    double yv[K];
     for (int r = 0; r < K; r++) {
-        float s = b[r];
+        double s = b[r];
         for (int m = 0; m < r; m++) s -= a[r * K + m] * yv[m];
         yv[r] = s / a[r * K + r];
     }
     for (int r = K - 1; r >= 0; r--) {
-        float s = yv[r];
+        double s = yv[r];
         for (int m = r + 1; m < K; m++) s -= a[m * K + r] * x[m];
         x[r] = s / a[r * K + r];
     }
     return true;
+}
+
+// Normal equations of the (scaled) exponential model over the trace: model
+// values in FP32, per-lane sums in FP32 (32 points), warp sums, the solve and
+// the parameters in FP64 -- the A, tau, C problem is ill-conditioned when
+// the decay is slow, and FP32 sums/solves do not reach its minimum.
+template <int K>
+__device__ double exp_normal(const float *y, int n, double frametime, int ave, float iy, float it, const double *pd,
+                             double *A, double *g, int lane)
+{
+    constexpr int NA = K * (K + 1) / 2 + K;
+    float acc[NA];
+    float pp[K];
+    for (int a = 0; a < K; a++) pp[a] = (float)pd[a];
+    for (int i = 0; i < NA; i++) acc[i] = 0.f;
+    double c2 = 0.0;
+    for (int x = lane; x < n; x += 32) {
+        float t = (float)(frametime * (x + 0.5) * ave) * it;
+        float f, gr[K];
+        exp_eval<K>(pp, t, f, gr);
+        double rd = (double)(__ldg(&y[x]) * iy) - (double)f;
+        float r = (float)rd;
+        int q = 0;
+        for (int a = 0; a < K; a++)
+            for (int b = 0; b <= a; b++) acc[q++] += gr[a] * gr[b];
+        for (int a = 0; a < K; a++) acc[q++] += gr[a] * r;
+        c2 += rd * rd;
+    }
+    int q = 0;
+    for (int a = 0; a < K; a++)
+        for (int b = 0; b <= a; b++) {
+            double v = warp_sum_d((double)acc[q++]);
+            A[a * K + b] = v;
+            A[b * K + a] = v;
+        }
+    for (int a = 0; a < K; a++) g[a] = warp_sum_d((double)acc[q++]);
+    return warp_sum_d(c2);
 }
 
 template <int K>
@@ -180,96 +217,60 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     const int n = j.nopit;
     const float *y = trace + (size_t)tr * n;
     const float tmax = (float)(j.frametime_d * (n - 0.5) * j.ave);
-    // scale of y
     float ym = 0.f;
     for (int x = lane; x < n; x += 32) ym = fmaxf(ym, fabsf(__ldg(&y[x])));
     for (int o = 16; o > 0; o >>= 1) ym = fmaxf(ym, __shfl_xor_sync(0xffffffffu, ym, o));
     if (ym == 0.f) ym = 1.f;
     const float iy = 1.f / ym, it = 1.f / tmax;
-    float p[K];
+    double p[K];
     {
-        float y1 = __ldg(&y[1]) * iy;
-        float thalf = (float)(j.frametime_d * (n / 2 + 0.5) * j.ave) * it;
-        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.f; }
+        // Java initial guesses (java:10862-10864, 10917-10921), scaled
+        double y1 = (double)(__ldg(&y[1]) * iy);
+        double thalf = j.frametime_d * (n / 2 + 0.5) * j.ave * it;
+        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.0; }
         else {
-            float t10 = (float)(j.frametime_d * (n / 10 + 0.5) * j.ave) * it;
-            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.f;
+            double t10 = j.frametime_d * (n / 10 + 0.5) * j.ave * it;
+            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.0;
         }
     }
-    float lambda = 1e-3f, chi2 = 0.f;
-    float A[K * K], g[K];
-    bool ok = true;
-    auto accumulate = [&](const float *pp, float *AA, float *gg) -> float {
-        float c2 = 0.f;
-        float acc[K * (K + 1) / 2 + K + 1];
-        for (int i = 0; i < K * (K + 1) / 2 + K + 1; i++) acc[i] = 0.f;
-        for (int x = lane; x < n; x += 32) {
-            float t = (float)(j.frametime_d * (x + 0.5) * j.ave) * it;
-            float f, gr[K];
-            exp_eval<K>(pp, t, f, gr);
-            float r = __ldg(&y[x]) * iy - f;
-            int q = 0;
-            for (int a = 0; a < K; a++)
-                for (int b = 0; b <= a; b++) acc[q++] += gr[a] * gr[b];
-            for (int a = 0; a < K; a++) acc[q++] += gr[a] * r;
-            acc[q] += r * r;
-        }
-        for (int i = 0; i < K * (K + 1) / 2 + K + 1; i++) acc[i] = warp_sum(acc[i]);
-        int q = 0;
-        if (AA) {
-            for (int a = 0; a < K; a++)
-                for (int b = 0; b <= a; b++) { AA[a * K + b] = acc[q]; AA[b * K + a] = acc[q]; q++; }
-            for (int a = 0; a < K; a++) gg[a] = acc[q++];
-        } else q += K * (K + 1) / 2 + K;
-        c2 = acc[q];
-        return c2;
-    };
-    chi2 = accumulate(p, A, g);
-    if (!isfinite(chi2)) ok = false;
-    int it_n = 0;
-    for (it_n = 0; ok && it_n < 300; it_n++) {
-        float M[K * K], h[K], pn[K];
-        float dmax = 0.f;
-        for (int a = 0; a < K; a++) dmax = fmaxf(dmax, A[a * K + a]);
+    double A[K * K], g[K], lambda = 1e-3;
+    double chi2 = exp_normal<K>(y, n, j.frametime_d, j.ave, iy, it, p, A, g, lane);
+    bool ok = isfinite(chi2);
+    for (int it_n = 0; ok && it_n < 300; it_n++) {
+        double M[K * K], h[K], pn[K], dmax = 0.0;
+        for (int a = 0; a < K; a++) dmax = fmax(dmax, A[a * K + a]);
         // converged when the undamped Gauss-Newton step is negligible
-        {
-            for (int a = 0; a < K * K; a++) M[a] = A[a];
-            for (int a = 0; a < K; a++) M[a * K + a] += 1e-12f * dmax;
-            if (solve_spd<K>(M, g, h)) {
-                bool conv = true;
-                for (int a = 0; a < K; a++) conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(p[a]) + 1e-6f;
-                if (conv) break;
-            }
+        for (int a = 0; a < K * K; a++) M[a] = A[a];
+        for (int a = 0; a < K; a++) M[a * K + a] += 1e-14 * dmax;
+        if (solve_spd<K>(M, g, h)) {
+            bool conv = true;
+            for (int a = 0; a < K; a++) conv = conv && fabs(h[a]) <= 1e-9 * fabs(p[a]) + 1e-9;
+            if (conv) break;
         }
         for (int a = 0; a < K * K; a++) M[a] = A[a];
-        // Marquardt damping with a floor so that a zero column (e.g. a zero
-        // initial amplitude) still gives a solvable system
-        for (int a = 0; a < K; a++) M[a * K + a] += lambda * fmaxf(A[a * K + a], 1e-6f * dmax);
-        if (!solve_spd<K>(M, g, h)) { lambda *= 10.f; if (lambda > 1e20f) break; continue; }
-        float rel = 0.f;
-        for (int a = 0; a < K; a++) {
-            pn[a] = p[a] + h[a];
-            rel = fmaxf(rel, fabsf(h[a]) / fmaxf(fabsf(p[a]), 1e-6f));
-        }
-        float An[K * K], gn[K];
-        float c2n = accumulate(pn, An, gn);
+        // Marquardt damping with a floor: a zero column (e.g. a zero initial
+        // amplitude) still gives a solvable system
+        for (int a = 0; a < K; a++) M[a * K + a] += lambda * fmax(A[a * K + a], 1e-6 * dmax);
+        if (!solve_spd<K>(M, g, h)) { lambda *= 10.0; if (lambda > 1e20) break; continue; }
+        for (int a = 0; a < K; a++) pn[a] = p[a] + h[a];
+        double An[K * K], gn[K];
+        double c2n = exp_normal<K>(y, n, j.frametime_d, j.ave, iy, it, pn, An, gn, lane);
         if (isfinite(c2n) && c2n < chi2) {
             for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
             for (int a = 0; a < K * K; a++) A[a] = An[a];
             chi2 = c2n;
-            lambda = fmaxf(lambda * 0.1f, 1e-9f);
-            (void)rel;
+            lambda = fmax(lambda * 0.1, 1e-12);
         } else {
-            lambda *= 10.f;
-            if (lambda > 1e12f) break;
+            lambda *= 10.0;
+            if (lambda > 1e12) break;
         }
     }
     // back to data units
     float res[5];
-    if (K == 3) { res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; }
+    if (K == 3) { res[0] = (float)(p[0] * ym); res[1] = (float)(p[1] * tmax); res[2] = (float)(p[2] * ym); }
     else {
-        res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; res[3] = p[3] * tmax;
-        res[4] = p[4] * ym;
+        res[0] = (float)(p[0] * ym); res[1] = (float)(p[1] * tmax); res[2] = (float)(p[2] * ym);
+        res[3] = (float)(p[3] * tmax); res[4] = (float)(p[4] * ym);
     }
     bool valid = ok;
     for (int a = 0; a < K; a++) valid = valid && isfinite(res[a]);
