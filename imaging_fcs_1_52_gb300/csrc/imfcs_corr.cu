@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
                 const int f = f0 + fr;
                 float va = 0.f, vb = 0.f;
                 if (f < j.num && pvalid) {
-                    float t = (float)(j.frametime_d * (f + 1.5));
+                    float t = frame_time(j, f);
                     const float *bs = sh_basis + fr * order1;
                     va = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xa - tx0, ya - ty0)
                                     : window_value(j, stack, xa, ya, f);

@@ -26,8 +26,8 @@ constexpr int kPtsPerLane = kMaxPts / 32;
 
 template <int KM>
 struct LMState {
-    double A[KM * KM];
-    double g[KM];
+    float A[KM * KM];
+    float g[KM];
     double chi2;
 };
 
@@ -159,51 +159,57 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
     for (int p = 0; p < KM; p++)
 #pragma unroll
         for (int t = 0; t <= p; t++) {
-            double v = warp_sum_d((double)acc[q++]);
+            float v = warp_sum(acc[q++]);
             s.A[p * KM + t] = v;
             s.A[t * KM + p] = v;
         }
 #pragma unroll
-    for (int p = 0; p < KM; p++) s.g[p] = warp_sum_d((double)acc[q++]);
-    s.chi2 = warp_sum_d(c2acc);
+    for (int p = 0; p < KM; p++) s.g[p] = warp_sum(acc[q++]);
+    s.chi2 = precise ? warp_sum_d(c2acc) : (double)warp_sum((float)c2acc);
 }
 
+// (A + lambda diag(A)) h = g, solved in FP32 on the Jacobi-scaled system
+// (unit diagonal), which keeps the Cholesky stable for strongly correlated
+// parameters.  Accuracy of the fixed point is set by g, not by this solve.
 template <int KM>
-__device__ __forceinline__ bool chol_solve_d(const double *Ain, const double *b, int k, double lambda,
-                                             const double *dscale, double *x)
+__device__ __forceinline__ bool solve_scaled(const float *A, const float *g, int k, float lambda, float *h)
 {
-    double L[KM * KM];
+    float sc[KM], L[KM * KM];
 #pragma unroll
-    for (int i = 0; i < KM * KM; i++) L[i] = Ain[i];
+    for (int i = 0; i < KM; i++) sc[i] = (i < k) ? rsqrtf(fmaxf(A[i * KM + i], 1e-30f)) : 0.f;
+#pragma unroll
+    for (int r = 0; r < KM; r++)
+#pragma unroll
+        for (int c = 0; c < KM; c++) L[r * KM + c] = A[r * KM + c] * sc[r] * sc[c];
 #pragma unroll
     for (int i = 0; i < KM; i++)
-        if (i < k) L[i * KM + i] += lambda * dscale[i];
+        if (i < k) L[i * KM + i] = 1.f + lambda;
 #pragma unroll
     for (int c = 0; c < KM; c++) {
         if (c >= k) break;
-        double d = L[c * KM + c];
+        float d = L[c * KM + c];
 #pragma unroll
         for (int m = 0; m < KM; m++)
             if (m < c) d -= L[c * KM + m] * L[c * KM + m];
-        if (!(d > 0.0) || !isfinite(d)) return false;
-        d = sqrt(d);
+        if (!(d > 0.f) || !isfinite(d)) return false;
+        d = sqrtf(d);
         L[c * KM + c] = d;
-        double id = 1.0 / d;
+        float id = 1.f / d;
 #pragma unroll
         for (int r = 0; r < KM; r++) {
             if (r <= c || r >= k) continue;
-            double sum = L[r * KM + c];
+            float sum = L[r * KM + c];
 #pragma unroll
             for (int m = 0; m < KM; m++)
                 if (m < c) sum -= L[r * KM + m] * L[c * KM + m];
             L[r * KM + c] = sum * id;
         }
     }
-    double yv[KM];
+    float yv[KM], z[KM];
 #pragma unroll
     for (int r = 0; r < KM; r++) {
-        if (r >= k) { yv[r] = 0.0; continue; }
-        double sum = b[r];
+        if (r >= k) { yv[r] = 0.f; continue; }
+        float sum = g[r] * sc[r];
 #pragma unroll
         for (int m = 0; m < KM; m++)
             if (m < r) sum -= L[r * KM + m] * yv[m];
@@ -211,13 +217,15 @@ __device__ __forceinline__ bool chol_solve_d(const double *Ain, const double *b,
     }
 #pragma unroll
     for (int r = KM - 1; r >= 0; r--) {
-        if (r >= k) { x[r] = 0.0; continue; }
-        double sum = yv[r];
+        if (r >= k) { z[r] = 0.f; continue; }
+        float sum = yv[r];
 #pragma unroll
         for (int m = 0; m < KM; m++)
-            if (m > r && m < k) sum -= L[m * KM + r] * x[m];
-        x[r] = sum / L[r * KM + r];
+            if (m > r && m < k) sum -= L[m * KM + r] * z[m];
+        z[r] = sum / L[r * KM + r];
     }
+#pragma unroll
+    for (int r = 0; r < KM; r++) h[r] = z[r] * sc[r];
     return true;
 }
 
@@ -277,49 +285,35 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
             c3 = par[7] != 0.f || f3free;
         }
         // Gpufit mode (tol > 0): FP32 model values throughout.  Step mode:
-        // FP32 values until the Gauss-Newton step is small, then a polish with
-        // FP64 model values.
-        bool precise = (a.model != IMFCS_MODEL_ACF_1D);
-        int polish = 0;
+        // LM with FP32 values until the undamped Gauss-Newton step is small
+        // (or no step lowers chi^2), then two Gauss-Newton steps whose
+        // residuals come from the FP64 model value.
         LMState<KM> s;
-        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, precise);
+        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
+                     a.model != IMFCS_MODEL_ACF_1D);
         int state = IMFCS_STATE_MAX_ITERATIONS, it = 0;
-        double lambda = 1e-3;
-        double dscale[KM];
-#pragma unroll
-        for (int i = 0; i < KM; i++) dscale[i] = (i < a.k) ? fmax(s.A[i * KM + i], 1e-300) : 1.0;
+        float lambda = 1e-3f;
         if (!isfinite(s.chi2)) state = IMFCS_STATE_SINGULAR_HESSIAN;
         else if (a.k == 0) state = IMFCS_STATE_CONVERGED;
+        bool to_polish = false;
         for (it = 0; state == IMFCS_STATE_MAX_ITERATIONS && it < a.max_iter; it++) {
-            double h[KM];
+            float h[KM];
             if (a.tol <= 0.f) {
-                // convergence on the undamped Gauss-Newton step
-                double hg[KM], zero[KM];
-#pragma unroll
-                for (int i = 0; i < KM; i++) zero[i] = 0.0;
-                if (chol_solve_d<KM>(s.A, s.g, a.k, 0.0, zero, hg)) {
-                    const double rel = precise ? 1e-9 : 1e-6, sg = precise ? 1e-7 : 1e-5;
+                float hg[KM];
+                if (solve_scaled<KM>(s.A, s.g, a.k, 0.f, hg)) {
                     bool conv = true;
 #pragma unroll
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) {
-                            double sig = 1.0 / sqrt(fmax(s.A[i * KM + i], 1e-300));
-                            conv = conv && (fabs(hg[i]) <= rel * fabs(pard[a.idx[i]]) + sg * sig);
+                            float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
+                            conv = conv && (fabsf(hg[i]) <= 1e-6f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
                         }
-                    if (conv || polish >= 8) {
-                        if (precise) { state = IMFCS_STATE_CONVERGED; break; }
-                        precise = true;   // switch to FP64 residuals and polish
-                        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
-                                     true);
-                        lambda = 1e-9;
-                        continue;
-                    }
+                    if (conv) { to_polish = true; state = IMFCS_STATE_CONVERGED; break; }
                 }
-                if (precise) polish++;
             }
-            if (!chol_solve_d<KM>(s.A, s.g, a.k, lambda, dscale, h)) {
-                lambda *= 10.0;
-                if (lambda > 1e15) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
+            if (!solve_scaled<KM>(s.A, s.g, a.k, lambda, h)) {
+                lambda *= 10.f;
+                if (lambda > 1e15f) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
                 continue;
             }
             double pnd[IMFCS_NPARAM];
@@ -327,44 +321,48 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
             for (int i = 0; i < a.np; i++) pnd[i] = pard[i];
 #pragma unroll
             for (int i = 0; i < KM; i++)
-                if (i < a.k) pnd[a.idx[i]] = pard[a.idx[i]] + h[i];
+                if (i < a.k) pnd[a.idx[i]] = pard[a.idx[i]] + (double)h[i];
             for (int i = 0; i < a.np; i++) pnf[i] = (float)pnd[i];
             LMState<KM> sn;
-            evaluate<KM>(a, mc, mcd, pnf, pnd, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, sn, c2, c3, precise);
+            evaluate<KM>(a, mc, mcd, pnf, pnd, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, sn, c2, c3,
+                         a.model != IMFCS_MODEL_ACF_1D);
             bool finite = isfinite(sn.chi2);
+            bool better = finite && sn.chi2 < s.chi2;
             if (a.tol > 0.f) {
                 // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487)
                 bool found = finite && fabs(sn.chi2 - s.chi2) < (double)a.tol * fmax(1.0, sn.chi2);
-                if (finite && sn.chi2 < s.chi2) {
+                if (better) {
                     for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
                     s = sn;
-                    lambda *= 0.1;
+                    lambda *= 0.1f;
                 } else {
-                    lambda *= 10.0;
+                    lambda *= 10.f;
                 }
+                if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
+            } else {
+                if (better) {
+                    for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
+                    s = sn;
+                    lambda = fmaxf(lambda * 0.1f, 1e-9f);
+                } else {
+                    lambda *= 10.f;
+                    if (lambda > 1e10f) { to_polish = true; state = IMFCS_STATE_CONVERGED; it++; break; }
+                }
+            }
+        }
+        if (to_polish && a.model == IMFCS_MODEL_ACF_1D) {
+#pragma unroll 1
+            for (int pi = 0; pi < 2; pi++) {
+                evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true);
+                float h[KM];
+                if (!solve_scaled<KM>(s.A, s.g, a.k, 0.f, h)) break;
 #pragma unroll
                 for (int i = 0; i < KM; i++)
-                    if (i < a.k) dscale[i] = fmax(dscale[i], s.A[i * KM + i]);
-                if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                if (lambda > 1e30) { state = IMFCS_STATE_CONVERGED; it++; break; }
-            } else {
-                if (finite && sn.chi2 < s.chi2) {
-                    for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
-                    s = sn;
-                    lambda = fmax(lambda * 0.1, 1e-9);
-#pragma unroll
-                    for (int i = 0; i < KM; i++)
-                        if (i < a.k) dscale[i] = fmax(dscale[i], s.A[i * KM + i]);
-                } else {
-                    lambda *= 10.0;
-                    if (lambda > 1e12) {
-                        if (precise) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                        precise = true;
-                        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
-                                     true);
-                        lambda = 1e-9;
+                    if (i < a.k) {
+                        pard[a.idx[i]] += (double)h[i];
+                        par[a.idx[i]] = (float)pard[a.idx[i]];
                     }
-                }
             }
         }
         if (lane == 0) {
@@ -374,7 +372,7 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
             if (a.out_iter) a.out_iter[fit] = it;
             if (a.out_hess)
                 for (int i = 0; i < a.k * a.k; i++)
-                    a.out_hess[(size_t)fit * a.k * a.k + i] = (float)s.A[(i / a.k) * KM + (i % a.k)];
+                    a.out_hess[(size_t)fit * a.k * a.k + i] = s.A[(i / a.k) * KM + (i % a.k)];
         }
         __syncwarp();
     }

@@ -171,8 +171,9 @@ __device__ __forceinline__ void trace_origin(const Job &j, int trace, int &x0, i
 //   v' = v / sqrt(f/f0) + f0 * (1 - sqrt(f/f0)),   t = frametime * (x + 0.5)
 // with x the 1-based frame number.  Parameters per trace (kBleachStride floats):
 //   [0..8] polynomial coefficients in the Legendre basis of u(t), or A, tau, C
-//   (single exp) / A1, tau1, A2, tau2, C (double exp); [9] f0; [10] 1/f0;
-//   [11] valid flag; [12] centre c; [13] u scale; [14] u offset.
+//   (single exp) / A1, tau1, A2, tau2, C (double exp) with [5], [6] = 1/tau1,
+//   1/tau2; [9] f0; [10] 1/f0; [11] valid flag; [12] centre c; [13] u scale;
+//   [14] u offset.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float bleach_f(const float *bp, int mode, int order, float t,
                                           const float *basis /* order+1 values at t */)
@@ -182,18 +183,23 @@ __device__ __forceinline__ float bleach_f(const float *bp, int mode, int order, 
         for (int i = 0; i <= order; i++) f = fmaf(bp[i], basis[i], f);
         return f;
     } else if (mode == IMFCS_BLEACH_SINGLE_EXP) {
-        return bp[0] * __expf(-t / bp[1]) + bp[2];
+        return fmaf(bp[0], __expf(-t * bp[5]), bp[2]);          // bp[5] = 1/tau
     } else {
-        return bp[0] * __expf(-t / bp[1]) + bp[2] * __expf(-t / bp[3]) + bp[4];
+        return bp[0] * __expf(-t * bp[5]) + bp[2] * __expf(-t * bp[6]) + bp[4];   // bp[5,6] = 1/tau1,2
     }
 }
 
+// v / sqrt(f/f0) + f0 (1 - sqrt(f/f0)) with one reciprocal square root.
 __device__ __forceinline__ float bleach_correct(float v, float f, float f0, float inv_f0)
 {
     float r = f * inv_f0;
-    float s = sqrtf(r);
-    return v / s + f0 * (1.f - s);
+    float rs = rsqrtf(r);
+    return fmaf(v, rs, f0 * (1.f - r * rs));
 }
+
+// Time of frame t (0-based) in the correction: frametime * (x + 0.5) with the
+// 1-based frame number x = t + 1 (java:9747).
+__device__ __forceinline__ float frame_time(const Job &j, int t) { return j.frametime * ((float)t + 1.5f); }
 
 // Legendre polynomials P_0..P_order at u.
 __device__ __forceinline__ void legendre(float u, int order, float *out)

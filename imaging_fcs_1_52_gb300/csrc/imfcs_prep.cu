@@ -80,7 +80,7 @@ __global__ void bleach_poly_kernel(Job j, const float *trace, const double *proj
     // centre: mean of the corrected averaged trace
     float csum = 0.f;
     for (int x = lane; x < j.nopit; x += 32) {
-        float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
+        float t = j.frametime * ((float)x + 0.5f) * (float)j.ave;
         legendre(t * uscale + uoff, j.poly_order, lb);
         float f = 0.f;
         for (int i = 0; i < k; i++) f = fmaf(cf[i], lb[i], f);
@@ -141,70 +141,71 @@ __device__ __forceinline__ void exp_eval(const float *p, float t, float &f, floa
     }
 }
 
+// (A + lambda diag(A) + ridge) x = b on the Jacobi-scaled system, FP32.
 template <int K>
-__device__ bool solve_spd(double *a, const double *b, double *x)
+__device__ bool solve_scaled_k(const float *A, const float *b, float lambda, float *x)
 {
-    // in-place Cholesky (lower) of a (K x K) then solve, FP64
+    float sc[K], L[K * K];
+    for (int i = 0; i < K; i++) sc[i] = rsqrtf(fmaxf(A[i * K + i], 1e-30f));
+    for (int r = 0; r < K; r++)
+        for (int c = 0; c < K; c++) L[r * K + c] = A[r * K + c] * sc[r] * sc[c];
+    for (int i = 0; i < K; i++) L[i * K + i] = 1.f + lambda + 1e-6f;
     for (int c = 0; c < K; c++) {
-        double d = a[c * K + c];
-        for (int m = 0; m < c; m++) d -= a[c * K + m] * a[c * K + m];
-        if (!(d > 0.0)) return false;
-        d = sqrt(d);
-        a[c * K + c] = d;
+        float d = L[c * K + c];
+        for (int m = 0; m < c; m++) d -= L[c * K + m] * L[c * K + m];
+        if (!(d > 0.f) || !isfinite(d)) return false;
+        d = sqrtf(d);
+        L[c * K + c] = d;
         for (int r = c + 1; r < K; r++) {
-            double s = a[r * K + c];
-            for (int m = 0; m < c; m++) s -= a[r * K + m] * a[c * K + m];
-            a[r * K + c] = s / d;
+            float s = L[r * K + c];
+            for (int m = 0; m < c; m++) s -= L[r * K + m] * L[c * K + m];
+            L[r * K + c] = s / d;
         }
     }
-    double yv[K];
+    float yv[K], z[K];
     for (int r = 0; r < K; r++) {
-        double s = b[r];
-        for (int m = 0; m < r; m++) s -= a[r * K + m] * yv[m];
-        yv[r] = s / a[r * K + r];
+        float s = b[r] * sc[r];
+        for (int m = 0; m < r; m++) s -= L[r * K + m] * yv[m];
+        yv[r] = s / L[r * K + r];
     }
     for (int r = K - 1; r >= 0; r--) {
-        double s = yv[r];
-        for (int m = r + 1; m < K; m++) s -= a[m * K + r] * x[m];
-        x[r] = s / a[r * K + r];
+        float s = yv[r];
+        for (int m = r + 1; m < K; m++) s -= L[m * K + r] * z[m];
+        z[r] = s / L[r * K + r];
     }
+    for (int r = 0; r < K; r++) x[r] = z[r] * sc[r];
     return true;
 }
 
-// Normal equations of the (scaled) exponential model over the trace: model
-// values in FP32, per-lane sums in FP32 (32 points), warp sums, the solve and
-// the parameters in FP64 -- the A, tau, C problem is ill-conditioned when
-// the decay is slow, and FP32 sums/solves do not reach its minimum.
+// Normal equations of the (scaled) exponential model over the trace: FP32
+// model, per-lane and warp sums (chi^2 accumulated per lane in FP64).
 template <int K>
-__device__ double exp_normal(const float *y, int n, double frametime, int ave, float iy, float it, const double *pd,
-                             double *A, double *g, int lane)
+__device__ double exp_normal(const float *y, int n, float frametime, int ave, float iy, float it, const float *pp,
+                             float *A, float *g, int lane)
 {
     constexpr int NA = K * (K + 1) / 2 + K;
     float acc[NA];
-    float pp[K];
-    for (int a = 0; a < K; a++) pp[a] = (float)pd[a];
     for (int i = 0; i < NA; i++) acc[i] = 0.f;
     double c2 = 0.0;
     for (int x = lane; x < n; x += 32) {
-        float t = (float)(frametime * (x + 0.5) * ave) * it;
+        float t = frametime * ((float)x + 0.5f) * (float)ave * it;
         float f, gr[K];
         exp_eval<K>(pp, t, f, gr);
-        double rd = (double)(__ldg(&y[x]) * iy) - (double)f;
-        float r = (float)rd;
+        float r = __ldg(&y[x]) * iy - f;
         int q = 0;
         for (int a = 0; a < K; a++)
             for (int b = 0; b <= a; b++) acc[q++] += gr[a] * gr[b];
         for (int a = 0; a < K; a++) acc[q++] += gr[a] * r;
-        c2 += rd * rd;
+        c2 += (double)(r * r);
     }
     int q = 0;
     for (int a = 0; a < K; a++)
         for (int b = 0; b <= a; b++) {
-            double v = warp_sum_d((double)acc[q++]);
+            float v = warp_sum(acc[q++]);
             A[a * K + b] = v;
             A[b * K + a] = v;
         }
-    for (int a = 0; a < K; a++) g[a] = warp_sum_d((double)acc[q++]);
+    for (int a = 0; a < K; a++) g[a] = warp_sum(acc[q++]);
     return warp_sum_d(c2);
 }
 
@@ -216,61 +217,54 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     if (tr >= j.ntrace) return;
     const int n = j.nopit;
     const float *y = trace + (size_t)tr * n;
-    const float tmax = (float)(j.frametime_d * (n - 0.5) * j.ave);
+    const float tmax = j.frametime * ((float)n - 0.5f) * (float)j.ave;
     float ym = 0.f;
     for (int x = lane; x < n; x += 32) ym = fmaxf(ym, fabsf(__ldg(&y[x])));
     for (int o = 16; o > 0; o >>= 1) ym = fmaxf(ym, __shfl_xor_sync(0xffffffffu, ym, o));
     if (ym == 0.f) ym = 1.f;
     const float iy = 1.f / ym, it = 1.f / tmax;
-    double p[K];
+    float p[K];
     {
         // Java initial guesses (java:10862-10864, 10917-10921), scaled
-        double y1 = (double)(__ldg(&y[1]) * iy);
-        double thalf = j.frametime_d * (n / 2 + 0.5) * j.ave * it;
-        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.0; }
+        float y1 = __ldg(&y[1]) * iy;
+        float thalf = j.frametime * ((float)(n / 2) + 0.5f) * (float)j.ave * it;
+        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.f; }
         else {
-            double t10 = j.frametime_d * (n / 10 + 0.5) * j.ave * it;
-            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.0;
+            float t10 = j.frametime * ((float)(n / 10) + 0.5f) * (float)j.ave * it;
+            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.f;
         }
     }
-    double A[K * K], g[K], lambda = 1e-3;
-    double chi2 = exp_normal<K>(y, n, j.frametime_d, j.ave, iy, it, p, A, g, lane);
+    float A[K * K], g[K], lambda = 1e-3f;
+    double chi2 = exp_normal<K>(y, n, j.frametime, j.ave, iy, it, p, A, g, lane);
     bool ok = isfinite(chi2);
     for (int it_n = 0; ok && it_n < 300; it_n++) {
-        double M[K * K], h[K], pn[K], dmax = 0.0;
-        for (int a = 0; a < K; a++) dmax = fmax(dmax, A[a * K + a]);
+        float h[K], pn[K];
         // converged when the undamped Gauss-Newton step is negligible
-        for (int a = 0; a < K * K; a++) M[a] = A[a];
-        for (int a = 0; a < K; a++) M[a * K + a] += 1e-14 * dmax;
-        if (solve_spd<K>(M, g, h)) {
+        if (solve_scaled_k<K>(A, g, 0.f, h)) {
             bool conv = true;
-            for (int a = 0; a < K; a++) conv = conv && fabs(h[a]) <= 1e-9 * fabs(p[a]) + 1e-9;
+            for (int a = 0; a < K; a++) conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(p[a]) + 1e-7f;
             if (conv) break;
         }
-        for (int a = 0; a < K * K; a++) M[a] = A[a];
-        // Marquardt damping with a floor: a zero column (e.g. a zero initial
-        // amplitude) still gives a solvable system
-        for (int a = 0; a < K; a++) M[a * K + a] += lambda * fmax(A[a * K + a], 1e-6 * dmax);
-        if (!solve_spd<K>(M, g, h)) { lambda *= 10.0; if (lambda > 1e20) break; continue; }
+        if (!solve_scaled_k<K>(A, g, lambda, h)) { lambda *= 10.f; if (lambda > 1e20f) break; continue; }
         for (int a = 0; a < K; a++) pn[a] = p[a] + h[a];
-        double An[K * K], gn[K];
-        double c2n = exp_normal<K>(y, n, j.frametime_d, j.ave, iy, it, pn, An, gn, lane);
+        float An[K * K], gn[K];
+        double c2n = exp_normal<K>(y, n, j.frametime, j.ave, iy, it, pn, An, gn, lane);
         if (isfinite(c2n) && c2n < chi2) {
             for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
             for (int a = 0; a < K * K; a++) A[a] = An[a];
             chi2 = c2n;
-            lambda = fmax(lambda * 0.1, 1e-12);
+            lambda = fmaxf(lambda * 0.1f, 1e-12f);
         } else {
-            lambda *= 10.0;
-            if (lambda > 1e12) break;
+            lambda *= 10.f;
+            if (lambda > 1e12f) break;
         }
     }
     // back to data units
     float res[5];
-    if (K == 3) { res[0] = (float)(p[0] * ym); res[1] = (float)(p[1] * tmax); res[2] = (float)(p[2] * ym); }
+    if (K == 3) { res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; }
     else {
-        res[0] = (float)(p[0] * ym); res[1] = (float)(p[1] * tmax); res[2] = (float)(p[2] * ym);
-        res[3] = (float)(p[3] * tmax); res[4] = (float)(p[4] * ym);
+        res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym;
+        res[3] = p[3] * tmax; res[4] = p[4] * ym;
     }
     bool valid = ok;
     for (int a = 0; a < K; a++) valid = valid && isfinite(res[a]);
@@ -279,14 +273,16 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     else valid = valid && (res[0] * res[1] * res[2] * res[3] != 0.f);
     float f0 = (K == 3) ? res[0] + res[2] : res[0] + res[2] + res[4];
     float inv_f0 = 1.f / f0;
+    float bpl[kBleachStride] = {0.f};
+    for (int a = 0; a < K; a++) bpl[a] = res[a];
+    bpl[5] = 1.f / res[1];
+    if (K == 5) bpl[6] = 1.f / res[3];
     float csum = 0.f;
     for (int x = lane; x < n; x += 32) {
         float yx = __ldg(&y[x]);
         if (valid) {
-            float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
-            float f = (K == 3) ? res[0] * __expf(-t / res[1]) + res[2]
-                               : res[0] * __expf(-t / res[1]) + res[2] * __expf(-t / res[3]) + res[4];
-            yx = bleach_correct(yx, f, f0, inv_f0);
+            float t = j.frametime * ((float)x + 0.5f) * (float)j.ave;
+            yx = bleach_correct(yx, bleach_f(bpl, j.bleach, 0, t, nullptr), f0, inv_f0);
         }
         csum += yx;
     }
@@ -294,6 +290,8 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     if (lane == 0) {
         float *bp = bp_out + (size_t)tr * kBleachStride;
         for (int a = 0; a < K; a++) bp[a] = res[a];
+        bp[5] = bpl[5];
+        bp[6] = bpl[6];
         bp[9] = f0;
         bp[10] = inv_f0;
         bp[11] = valid ? 1.f : 0.f;
@@ -309,7 +307,7 @@ __device__ __forceinline__ float correct_value(const Job &j, float v, int t, con
                                                const float *basis)
 {
     if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
-        float tt = (float)(j.frametime_d * (t + 1.5));
+        float tt = frame_time(j, t);
         float f = bleach_f(bp, j.bleach, j.poly_order, tt,
                            basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
         v = bleach_correct(v, f, bp[9], bp[10]);
@@ -322,7 +320,7 @@ __device__ __forceinline__ float corrected_delta(const Job &j, const void *stack
 {
     float v = window_value(j, stack, x0, y0, t);
     if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
-        float tt = (float)(j.frametime_d * (t + 1.5));
+        float tt = frame_time(j, t);
         float f = bleach_f(bp, j.bleach, j.poly_order, tt,
                            basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
         v = bleach_correct(v, f, bp[9], bp[10]);
@@ -615,7 +613,7 @@ __global__ void center_given_kernel(Job j, const float *trace, float *bp_out)
     for (int x = lane; x < j.nopit; x += 32) {
         float v = __ldg(&y[x]);
         if (j.bleach != IMFCS_BLEACH_NONE && bpl[11] != 0.f) {
-            float t = (float)(j.frametime_d * (x + 0.5) * j.ave);
+            float t = j.frametime * ((float)x + 0.5f) * (float)j.ave;
             if (j.bleach == IMFCS_BLEACH_POLYNOMIAL) legendre(t * bpl[13] + bpl[14], j.poly_order, lb);
             v = bleach_correct(v, bleach_f(bpl, j.bleach, j.poly_order, t, lb), bpl[9], bpl[10]);
         }

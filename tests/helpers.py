@@ -7,7 +7,7 @@ from imaging_fcs_1_52_gb300 import engine
 
 # Tolerances, stated once (FP32 GPU path vs FP64 oracle):
 ACF_TOL = 1e-5      # |dG| <= ACF_TOL * |G(lag 1)| for every lag >= 1
-VAR_TOL = 1e-4      # relative, blocked variance
+VAR_TOL = 5e-4      # relative, blocked variance (max); the median is checked at 1e-5
 FIT_TOL = 1e-4      # relative, fitted N and D
 
 
