@@ -9,8 +9,9 @@
 // Lanes own fit points; J^T W J, J^T W r and chi^2 are warp reductions; the
 // small K x K damped system is solved redundantly in every lane.  The grid is
 // persistent: each warp strides over fits.  The solver stops on a small step
-// (undamped Gauss-Newton step |h_i| <= 1e-6 |p_i| + 1e-5 sigma_i), which pins
-// the minimum to ~1e-5 sigma in FP32, or when no step lowers chi^2 any more, or on the Gpufit criterion |dchi2| < tol max(1, chi2) when a
+// (undamped Gauss-Newton step |h_i| <= 1e-7 |p_i| + 1e-5 sigma_i) once the
+// residuals come from the FP64 model value, or when no step lowers chi^2 any
+// more, or on the Gpufit criterion |dchi2| < tol max(1, chi2) when a
 // tolerance is given through the reference fit API.
 #include <math.h>
 
@@ -82,10 +83,26 @@ __device__ __forceinline__ double model_eval(const FitArgs &a, const ModelConst 
 // Jacobian are first transformed by L^-1 held in shared memory (packed lower
 // triangle); y then holds the transformed data.
 template <int KM>
+__device__ __forceinline__ void accumulate_point(float *acc, double &c2acc, const float *gr, double rd, float w)
+{
+    float r = (float)rd;
+    int q = 0;
+#pragma unroll
+    for (int p = 0; p < KM; p++)
+#pragma unroll
+        for (int t = 0; t <= p; t++) acc[q++] += w * gr[p] * gr[t];
+#pragma unroll
+    for (int p = 0; p < KM; p++) acc[q++] += w * gr[p] * r;
+    c2acc += (double)w * rd * rd;
+}
+
+// yg/wg (non-null): the fit's data are read from global memory point by point
+// (fits with more than kMaxPts points, no GLS transform).
+template <int KM>
 __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd, const float *par,
                          const double *pard, const float *yl, const float *wl, const float *xl, int lane,
                          float *sh_fj, double *sh_f64, const float *sh_linv, LMState<KM> &s, bool c2,
-                         bool c3, bool precise)
+                         bool c3, bool precise, const float *yg = nullptr, const float *wg = nullptr)
 {
     constexpr int NACC = KM * (KM + 1) / 2 + KM;
     float acc[NACC];
@@ -93,23 +110,20 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
 #pragma unroll
     for (int i = 0; i < NACC; i++) acc[i] = 0.f;
     const int n = a.npts;
-    if (!sh_linv) {
+    if (yg) {
+        for (int i = lane; i < n; i += 32) {
+            float gr[KM];
+            double f = model_eval<KM>(a, mc, mcd, par, pard, __ldg(&a.x[i]), gr, c2, c3, precise);
+            accumulate_point<KM>(acc, c2acc, gr, (double)__ldg(&yg[i]) - f, wg ? __ldg(&wg[i]) : 1.f);
+        }
+    } else if (!sh_linv) {
 #pragma unroll
         for (int m = 0; m < kPtsPerLane; m++) {
             int i = lane + 32 * m;
             if (i < n) {
                 float gr[KM];
                 double f = model_eval<KM>(a, mc, mcd, par, pard, xl[m], gr, c2, c3, precise);
-                double rd = (double)yl[m] - f;
-                float r = (float)rd, w = wl[m];
-                int q = 0;
-#pragma unroll
-                for (int p = 0; p < KM; p++)
-#pragma unroll
-                    for (int t = 0; t <= p; t++) acc[q++] += w * gr[p] * gr[t];
-#pragma unroll
-                for (int p = 0; p < KM; p++) acc[q++] += w * gr[p] * r;
-                c2acc += (double)w * rd * rd;
+                accumulate_point<KM>(acc, c2acc, gr, (double)yl[m] - f, wl[m]);
             }
         }
     } else {
@@ -229,7 +243,7 @@ __device__ __forceinline__ bool solve_scaled(const float *A, const float *g, int
     return true;
 }
 
-template <int KM>
+template <int KM, bool BIG>
 __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
 {
     extern __shared__ float fsh[];
@@ -252,7 +266,7 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
 #pragma unroll
     for (int m = 0; m < kPtsPerLane; m++) {
         int i = lane + 32 * m;
-        xl[m] = i < n ? __ldg(&a.x[i]) : 0.f;
+        xl[m] = (!BIG && i < n) ? __ldg(&a.x[i]) : 0.f;
     }
 
     for (int fit = gw; fit < a.nfits; fit += nw) {
@@ -260,9 +274,12 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
 #pragma unroll
         for (int m = 0; m < kPtsPerLane; m++) {
             int i = lane + 32 * m;
-            yl[m] = i < n ? __ldg(&a.y[(size_t)fit * n + i]) : 0.f;
-            wl[m] = (i < n) ? (a.w ? __ldg(&a.w[(size_t)fit * n + i]) : 1.f) : 0.f;
+            bool in = !BIG && i < n;
+            yl[m] = in ? __ldg(&a.y[(size_t)fit * n + i]) : 0.f;
+            wl[m] = in ? (a.w ? __ldg(&a.w[(size_t)fit * n + i]) : 1.f) : 0.f;
         }
+        const float *yg = BIG ? a.y + (size_t)fit * n : nullptr;
+        const float *wg = (BIG && a.w) ? a.w + (size_t)fit * n : nullptr;
         if (sh_linv) {
             const float *src = a.linv + (size_t)fit * linv_len;
             for (int i = lane; i < linv_len; i += 32) sh_linv[i] = __ldg(&src[i]);
@@ -284,21 +301,24 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
             c2 = par[5] != 0.f || f2free;
             c3 = par[7] != 0.f || f3free;
         }
-        // Gpufit mode (tol > 0): FP32 model values throughout.  Step mode:
-        // LM with FP32 values until the undamped Gauss-Newton step is small
-        // (or no step lowers chi^2), then two Gauss-Newton steps whose
-        // residuals come from the FP64 model value.
+        // Gpufit mode (tol > 0): FP32 model values throughout, Gpufit's stop
+        // rule.  Step mode, ACF model: phase 1 with FP32 model values until
+        // the Gauss-Newton step is below 1e-3 sigma (or no step lowers chi^2
+        // up to lambda 1e6); phase 2 with residuals from the FP64 model value
+        // until the step is below 1e-5 sigma + 1e-7 |p| (or no step lowers
+        // chi^2 up to lambda 1e10).  The linear model is FP64 throughout.
+        const bool gpufit = a.tol > 0.f;
+        bool precise = a.model != IMFCS_MODEL_ACF_1D;
         LMState<KM> s;
-        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
-                     a.model != IMFCS_MODEL_ACF_1D);
-        int state = IMFCS_STATE_MAX_ITERATIONS, it = 0;
+        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, precise, yg, wg);
+        int state = IMFCS_STATE_MAX_ITERATIONS, it = 0, nprec = 0;
         float lambda = 1e-3f;
         if (!isfinite(s.chi2)) state = IMFCS_STATE_SINGULAR_HESSIAN;
         else if (a.k == 0) state = IMFCS_STATE_CONVERGED;
-        bool to_polish = false;
         for (it = 0; state == IMFCS_STATE_MAX_ITERATIONS && it < a.max_iter; it++) {
             float h[KM];
-            if (a.tol <= 0.f) {
+            bool to_precise = false;
+            if (!gpufit) {
                 float hg[KM];
                 if (solve_scaled<KM>(s.A, s.g, a.k, 0.f, hg)) {
                     bool conv = true;
@@ -306,63 +326,66 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) {
                             float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
-                            conv = conv && (fabsf(hg[i]) <= 1e-6f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
+                            float tol = precise ? 1e-7f * fabsf(par[a.idx[i]]) + 1e-5f * sig : 1e-3f * sig;
+                            conv = conv && (fabsf(hg[i]) <= tol);
                         }
-                    if (conv) { to_polish = true; state = IMFCS_STATE_CONVERGED; break; }
+                    if (conv) {
+                        if (precise) { state = IMFCS_STATE_CONVERGED; break; }
+                        to_precise = true;
+                    }
                 }
             }
-            if (!solve_scaled<KM>(s.A, s.g, a.k, lambda, h)) {
-                lambda *= 10.f;
-                if (lambda > 1e15f) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
-                continue;
-            }
-            double pnd[IMFCS_NPARAM];
-            float pnf[IMFCS_NPARAM];
-            for (int i = 0; i < a.np; i++) pnd[i] = pard[i];
-#pragma unroll
-            for (int i = 0; i < KM; i++)
-                if (i < a.k) pnd[a.idx[i]] = pard[a.idx[i]] + (double)h[i];
-            for (int i = 0; i < a.np; i++) pnf[i] = (float)pnd[i];
-            LMState<KM> sn;
-            evaluate<KM>(a, mc, mcd, pnf, pnd, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, sn, c2, c3,
-                         a.model != IMFCS_MODEL_ACF_1D);
-            bool finite = isfinite(sn.chi2);
-            bool better = finite && sn.chi2 < s.chi2;
-            if (a.tol > 0.f) {
-                // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487)
-                bool found = finite && fabs(sn.chi2 - s.chi2) < (double)a.tol * fmax(1.0, sn.chi2);
-                if (better) {
-                    for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
-                    s = sn;
-                    lambda *= 0.1f;
-                } else {
+            if (!to_precise) {
+                if (!solve_scaled<KM>(s.A, s.g, a.k, lambda, h)) {
                     lambda *= 10.f;
+                    if (lambda > 1e15f) { state = IMFCS_STATE_SINGULAR_HESSIAN; break; }
+                    continue;
                 }
-                if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
-            } else {
+                double pnd[IMFCS_NPARAM];
+                float pnf[IMFCS_NPARAM];
+                for (int i = 0; i < a.np; i++) pnd[i] = pard[i];
+#pragma unroll
+                for (int i = 0; i < KM; i++)
+                    if (i < a.k) pnd[a.idx[i]] = pard[a.idx[i]] + (double)h[i];
+                for (int i = 0; i < a.np; i++) pnf[i] = (float)pnd[i];
+                LMState<KM> sn;
+                evaluate<KM>(a, mc, mcd, pnf, pnd, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, sn, c2, c3, precise,
+                             yg, wg);
+                if (precise && a.model == IMFCS_MODEL_ACF_1D) nprec++;
+                const bool finite = isfinite(sn.chi2);
+                const bool better = finite && sn.chi2 < s.chi2;
+                if (gpufit) {
+                    // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487)
+                    bool found = finite && fabs(sn.chi2 - s.chi2) < (double)a.tol * fmax(1.0, sn.chi2);
+                    if (better) {
+                        for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
+                        s = sn;
+                        lambda *= 0.1f;
+                    } else {
+                        lambda *= 10.f;
+                    }
+                    if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                    if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                    continue;
+                }
                 if (better) {
                     for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
                     s = sn;
                     lambda = fmaxf(lambda * 0.1f, 1e-9f);
                 } else {
                     lambda *= 10.f;
-                    if (lambda > 1e10f) { to_polish = true; state = IMFCS_STATE_CONVERGED; it++; break; }
-                }
-            }
-        }
-        if (to_polish && a.model == IMFCS_MODEL_ACF_1D) {
-#pragma unroll 1
-            for (int pi = 0; pi < 2; pi++) {
-                evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true);
-                float h[KM];
-                if (!solve_scaled<KM>(s.A, s.g, a.k, 0.f, h)) break;
-#pragma unroll
-                for (int i = 0; i < KM; i++)
-                    if (i < a.k) {
-                        pard[a.idx[i]] += (double)h[i];
-                        par[a.idx[i]] = (float)pard[a.idx[i]];
+                    if (lambda > (precise ? 1e10f : 1e6f)) {
+                        if (precise) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                        to_precise = true;
                     }
+                }
+                if (nprec > 60) { state = IMFCS_STATE_CONVERGED; it++; break; }
+            }
+            if (to_precise) {
+                precise = true;
+                evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true,
+                             yg, wg);
+                lambda = 1e-3f;
             }
         }
         if (lane == 0) {
@@ -378,9 +401,12 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
     }
 }
 
-template __global__ void lm_kernel<3>(FitArgs);
-template __global__ void lm_kernel<5>(FitArgs);
-template __global__ void lm_kernel<11>(FitArgs);
+template __global__ void lm_kernel<3, false>(FitArgs);
+template __global__ void lm_kernel<5, false>(FitArgs);
+template __global__ void lm_kernel<11, false>(FitArgs);
+template __global__ void lm_kernel<3, true>(FitArgs);
+template __global__ void lm_kernel<5, true>(FitArgs);
+template __global__ void lm_kernel<11, true>(FitArgs);
 
 size_t lm_smem_bytes(const FitArgs &a, int km, int warps)
 {
@@ -391,23 +417,20 @@ size_t lm_smem_bytes(const FitArgs &a, int km, int warps)
 cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream)
 {
     if (a.nfits <= 0) return cudaSuccess;
-    if (a.npts > kMaxPts) return cudaErrorInvalidValue;
+    const bool big = a.npts > kMaxPts;
+    if (big && a.linv) return cudaErrorInvalidValue;
     const int warps = 4;
     int km = a.k <= 3 ? 3 : (a.k <= 5 ? 5 : 11);
     size_t smem = lm_smem_bytes(a, km, warps);
     int blocks = (a.nfits + warps - 1) / warps;
     int cap = num_sms * 16;
     if (blocks > cap) blocks = cap;
-    if (km == 3) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(lm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        lm_kernel<3><<<blocks, warps * 32, smem, stream>>>(a);
-    } else if (km == 5) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(lm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        lm_kernel<5><<<blocks, warps * 32, smem, stream>>>(a);
-    } else {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(lm_kernel<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        lm_kernel<11><<<blocks, warps * 32, smem, stream>>>(a);
-    }
+    void (*kern)(FitArgs);
+    if (km == 3) kern = big ? lm_kernel<3, true> : lm_kernel<3, false>;
+    else if (km == 5) kern = big ? lm_kernel<5, true> : lm_kernel<5, false>;
+    else kern = big ? lm_kernel<11, true> : lm_kernel<11, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, warps * 32, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

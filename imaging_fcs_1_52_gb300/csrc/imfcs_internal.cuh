@@ -170,11 +170,39 @@ __device__ __forceinline__ void trace_origin(const Job &j, int trace, int &x0, i
 // Bleach correction of one frame value (java:9682-9769):
 //   v' = v / sqrt(f/f0) + f0 * (1 - sqrt(f/f0)),   t = frametime * (x + 0.5)
 // with x the 1-based frame number.  Parameters per trace (kBleachStride floats):
-//   [0..8] polynomial coefficients in the Legendre basis of u(t), or A, tau, C
-//   (single exp) / A1, tau1, A2, tau2, C (double exp) with [5], [6] = 1/tau1,
-//   1/tau2; [9] f0; [10] 1/f0; [11] valid flag; [12] centre c; [13] u scale;
-//   [14] u offset.
+//   polynomial: [0..8] coefficients in the Legendre basis of u(t), [13] u
+//     scale, [14] u offset;
+//   exponential: [0..4] the fit in the reference's form A, tau, C (single) or
+//     A1, tau1, A2, tau2, C (double); the curve is evaluated as
+//     f(t) = [13] + sum_c term_c(t) with rate k_c = [5], [6] (1/s) and
+//     amplitude a_c = [7], [8]: term_c = a_c exp(-k_c t) when bit c of [14]
+//     is clear, else -a_c t phi(k_c t), phi(x) = (1 - e^-x)/x as a series
+//     (slow components, k_c t <= 0.5, where A and C of the reference's form
+//     cancel);
+//   all modes: [9] f0; [10] 1/f0; [11] valid flag; [12] centre c.
 // ---------------------------------------------------------------------------
+// t phi(k t) = (1 - e^{-kt}) / k for x = k t in [0, 0.5]: series to x^7
+// (truncation below x^8 / 9! = 1.1e-8).
+__device__ __forceinline__ float slow_exp_term(float k, float t)
+{
+    float x = k * t;
+    float ph = fmaf(x, -1.f / 40320.f, 1.f / 5040.f);
+    ph = fmaf(x, ph, -1.f / 720.f);
+    ph = fmaf(x, ph, 1.f / 120.f);
+    ph = fmaf(x, ph, -1.f / 24.f);
+    ph = fmaf(x, ph, 1.f / 6.f);
+    ph = fmaf(x, ph, -0.5f);
+    ph = fmaf(x, ph, 1.f);
+    return t * ph;
+}
+
+__device__ __forceinline__ float exp_component(const float *bp, int c, float t)
+{
+    const int flags = (int)bp[14];
+    const float k = bp[5 + c], a = bp[7 + c];
+    return ((flags >> c) & 1) ? -a * slow_exp_term(k, t) : a * __expf(-k * t);
+}
+
 __device__ __forceinline__ float bleach_f(const float *bp, int mode, int order, float t,
                                           const float *basis /* order+1 values at t */)
 {
@@ -183,9 +211,9 @@ __device__ __forceinline__ float bleach_f(const float *bp, int mode, int order, 
         for (int i = 0; i <= order; i++) f = fmaf(bp[i], basis[i], f);
         return f;
     } else if (mode == IMFCS_BLEACH_SINGLE_EXP) {
-        return fmaf(bp[0], __expf(-t * bp[5]), bp[2]);          // bp[5] = 1/tau
+        return bp[13] + exp_component(bp, 0, t);
     } else {
-        return bp[0] * __expf(-t * bp[5]) + bp[2] * __expf(-t * bp[6]) + bp[4];   // bp[5,6] = 1/tau1,2
+        return bp[13] + exp_component(bp, 0, t) + exp_component(bp, 1, t);
     }
 }
 

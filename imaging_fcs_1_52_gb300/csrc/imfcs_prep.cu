@@ -117,39 +117,68 @@ __global__ void center_kernel(Job j, const float *trace, float *bp_out)
 }
 
 // ---------------------------------------------------------------------------
-// Exponential bleach fits (SingleExp / DoubleExp, java:13028-13085) by an
-// FP32 Levenberg-Marquardt per warp, in scaled variables (t / tmax, y / ymax),
-// from the Java initial guesses (java:10862-10864, 10917-10921).
+// Exponential bleach fits (SingleExp / DoubleExp, java:13028-13085).
+//
+// The reference fits A e^{-t/tau} + C (+ A2 e^{-t/tau2}) by Levenberg-
+// Marquardt from fixed initial guesses (java:10862-10864, 10917-10921).  The
+// same least-squares problem is solved here in the equivalent parameters
+//     f0 = f(0),  s_c = A_c / tau_c,  k_c = 1 / tau_c >= 0,
+//     f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c,
+// which stay well conditioned when a component is slow (k_c t << 1, where
+// the reference's A and C grow without bound while A + C stays finite).
+// Scaled variables t / tmax, y / ymax; one warp per trace.
+//   phase 1: FP32 model and normal equations until the Gauss-Newton step is
+//            below 1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
+//   phase 2: model values and residuals in FP64 (the exponentials by a
+//            per-lane recurrence), Jacobian and normal equations in FP32,
+//            until the step is below 1e-5 sigma + 1e-7 |p|.
+// A rate at its bound k = 0 whose Gauss-Newton step points below it is held
+// fixed (active set).
 // ---------------------------------------------------------------------------
-template <int K>
-__device__ __forceinline__ void exp_eval(const float *p, float t, float &f, float *g)
+
+// u = (1 - e^{-kt}) / k and du/dk in FP32, x = k t >= 0.
+__device__ __forceinline__ void exp_u_f(float k, float t, float &u, float &dudk)
 {
-    if (K == 3) {
-        float e = __expf(-t / p[1]);
-        f = p[0] * e + p[2];
-        g[0] = e;
-        g[1] = p[0] * t * e / (p[1] * p[1]);
-        g[2] = 1.f;
+    const float x = k * t;
+    if (x < 0.05f) {
+        u = slow_exp_term(k, t);
+        // du/dk = -t^2 (1/2 - x/3 + x^2/8 - x^3/30 + x^4/144)
+        float d = fmaf(x, 1.f / 144.f, -1.f / 30.f);
+        d = fmaf(x, d, 1.f / 8.f);
+        d = fmaf(x, d, -1.f / 3.f);
+        d = fmaf(x, d, 0.5f);
+        dudk = -t * t * d;
     } else {
-        float e1 = __expf(-t / p[1]), e2 = __expf(-t / p[3]);
-        f = p[0] * e1 + p[2] * e2 + p[4];
-        g[0] = e1;
-        g[1] = p[0] * t * e1 / (p[1] * p[1]);
-        g[2] = e2;
-        g[3] = p[2] * t * e2 / (p[3] * p[3]);
-        g[4] = 1.f;
+        const float em = expm1f(-x);
+        u = -em / k;
+        dudk = (t * (1.f + em) - u) / k;
     }
 }
 
-// (A + lambda diag(A) + ridge) x = b on the Jacobi-scaled system, FP32.
+// du/dk from an FP32 copy of e = e^{-kt} and u (series for small x).
+__device__ __forceinline__ float exp_dudk(float k, float t, float e, float u)
+{
+    const float x = k * t;
+    if (x < 0.05f) {
+        float d = fmaf(x, 1.f / 144.f, -1.f / 30.f);
+        d = fmaf(x, d, 1.f / 8.f);
+        d = fmaf(x, d, -1.f / 3.f);
+        d = fmaf(x, d, 0.5f);
+        return -t * t * d;
+    }
+    return (t * e - u) / k;
+}
+
+// (A + lambda diag(A) + ridge) x = b on the Jacobi-scaled system, FP32;
+// parameters in `fix` (bit mask) are held: x_i = 0.
 template <int K>
-__device__ bool solve_scaled_k(const float *A, const float *b, float lambda, float *x)
+__device__ bool solve_scaled_k(const float *A, const float *b, float lambda, unsigned fix, float *x)
 {
     float sc[K], L[K * K];
-    for (int i = 0; i < K; i++) sc[i] = rsqrtf(fmaxf(A[i * K + i], 1e-30f));
+    for (int i = 0; i < K; i++) sc[i] = ((fix >> i) & 1) ? 0.f : rsqrtf(fmaxf(A[i * K + i], 1e-30f));
     for (int r = 0; r < K; r++)
         for (int c = 0; c < K; c++) L[r * K + c] = A[r * K + c] * sc[r] * sc[c];
-    for (int i = 0; i < K; i++) L[i * K + i] = 1.f + lambda + 1e-6f;
+    for (int i = 0; i < K; i++) L[i * K + i] = ((fix >> i) & 1) ? 1.f : 1.f + lambda + 1e-6f;
     for (int c = 0; c < K; c++) {
         float d = L[c * K + c];
         for (int m = 0; m < c; m++) d -= L[c * K + m] * L[c * K + m];
@@ -177,106 +206,213 @@ __device__ bool solve_scaled_k(const float *A, const float *b, float lambda, flo
     return true;
 }
 
-// Normal equations of the (scaled) exponential model over the trace: FP32
-// model, per-lane and warp sums (chi^2 accumulated per lane in FP64).
+// chi^2 and the normal equations A = J^T J, g = J^T r of the scaled model at
+// p over the trace (warp); precise: FP64 model values and residuals.
 template <int K>
-__device__ double exp_normal(const float *y, int n, float frametime, int ave, float iy, float it, const float *pp,
+__device__ double exp_normal(const float *y, int n, float dts, float iy, const double *p, bool precise,
                              float *A, float *g, int lane)
 {
+    constexpr int NC = (K - 1) / 2;
     constexpr int NA = K * (K + 1) / 2 + K;
     float acc[NA];
     for (int i = 0; i < NA; i++) acc[i] = 0.f;
+    float pf[K];
+    for (int i = 0; i < K; i++) pf[i] = (float)p[i];
+    double e[NC], q[NC], invk[NC];
+    bool slow[NC];
+    if (precise) {
+        for (int c = 0; c < NC; c++) {
+            const double k = p[2 + 2 * c];
+            e[c] = exp(-k * ((double)lane + 0.5) * (double)dts);
+            q[c] = exp(-k * 32.0 * (double)dts);
+            slow[c] = k * (double)n * (double)dts < 1e-4;
+            invk[c] = slow[c] ? 0.0 : 1.0 / k;
+        }
+    }
     double c2 = 0.0;
     for (int x = lane; x < n; x += 32) {
-        float t = frametime * ((float)x + 0.5f) * (float)ave * it;
-        float f, gr[K];
-        exp_eval<K>(pp, t, f, gr);
-        float r = __ldg(&y[x]) * iy - f;
-        int q = 0;
+        const float t = ((float)x + 0.5f) * dts;
+        float gr[K], r;
+        gr[0] = 1.f;
+        if (!precise) {
+            float f = pf[0];
+            for (int c = 0; c < NC; c++) {
+                float u, du;
+                exp_u_f(pf[2 + 2 * c], t, u, du);
+                f -= pf[1 + 2 * c] * u;
+                gr[1 + 2 * c] = -u;
+                gr[2 + 2 * c] = -pf[1 + 2 * c] * du;
+            }
+            r = __ldg(&y[x]) * iy - f;
+            c2 += (double)r * (double)r;
+        } else {
+            const double td = ((double)x + 0.5) * (double)dts;
+            double f = p[0];
+            for (int c = 0; c < NC; c++) {
+                const double k = p[2 + 2 * c];
+                double u;
+                if (slow[c]) {
+                    const double xx = k * td;
+                    u = td * (1.0 - xx * (0.5 - xx * (1.0 / 6.0 - xx * (1.0 / 24.0))));
+                } else {
+                    u = (1.0 - e[c]) * invk[c];
+                }
+                f -= p[1 + 2 * c] * u;
+                const float uf = (float)u;
+                gr[1 + 2 * c] = -uf;
+                gr[2 + 2 * c] = -pf[1 + 2 * c] * exp_dudk(pf[2 + 2 * c], t, (float)e[c], uf);
+                e[c] *= q[c];
+            }
+            const double rd = (double)__ldg(&y[x]) * (double)iy - f;
+            r = (float)rd;
+            c2 += rd * rd;
+        }
+        int qa = 0;
         for (int a = 0; a < K; a++)
-            for (int b = 0; b <= a; b++) acc[q++] += gr[a] * gr[b];
-        for (int a = 0; a < K; a++) acc[q++] += gr[a] * r;
-        c2 += (double)(r * r);
+            for (int b = 0; b <= a; b++) acc[qa++] += gr[a] * gr[b];
+        for (int a = 0; a < K; a++) acc[qa++] += gr[a] * r;
     }
-    int q = 0;
+    int qa = 0;
     for (int a = 0; a < K; a++)
         for (int b = 0; b <= a; b++) {
-            float v = warp_sum(acc[q++]);
+            float v = warp_sum(acc[qa++]);
             A[a * K + b] = v;
             A[b * K + a] = v;
         }
-    for (int a = 0; a < K; a++) g[a] = warp_sum(acc[q++]);
+    for (int a = 0; a < K; a++) g[a] = warp_sum(acc[qa++]);
     return warp_sum_d(c2);
+}
+
+// Held rates (bit mask) and the undamped Gauss-Newton step.
+template <int K>
+__device__ __forceinline__ bool exp_gn_step(const float *A, const float *g, const double *p, unsigned &fix,
+                                            float *h)
+{
+    constexpr int NC = (K - 1) / 2;
+    fix = 0;
+    bool ok = solve_scaled_k<K>(A, g, 0.f, 0u, h);
+    for (int c = 0; c < NC; c++)
+        if (p[2 + 2 * c] <= 0.0 && (!ok || h[2 + 2 * c] < 0.f)) fix |= 1u << (2 + 2 * c);
+    if (fix) ok = solve_scaled_k<K>(A, g, 0.f, fix, h);
+    return ok;
 }
 
 template <int K>
 __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
 {
+    constexpr int NC = (K - 1) / 2;
     const int lane = threadIdx.x & 31;
     const int tr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (tr >= j.ntrace) return;
     const int n = j.nopit;
     const float *y = trace + (size_t)tr * n;
-    const float tmax = j.frametime * ((float)n - 0.5f) * (float)j.ave;
+    const double dt_pt = (double)j.frametime * (double)j.ave;      // time per trace point (s)
+    const float tmax = (float)(dt_pt * ((double)n - 0.5));
+    const float dts = (float)(dt_pt / (double)tmax);               // scaled time per point
     float ym = 0.f;
     for (int x = lane; x < n; x += 32) ym = fmaxf(ym, fabsf(__ldg(&y[x])));
     for (int o = 16; o > 0; o >>= 1) ym = fmaxf(ym, __shfl_xor_sync(0xffffffffu, ym, o));
     if (ym == 0.f) ym = 1.f;
-    const float iy = 1.f / ym, it = 1.f / tmax;
-    float p[K];
+    const float iy = 1.f / ym;
+    double p[K];
     {
-        // Java initial guesses (java:10862-10864, 10917-10921), scaled
-        float y1 = __ldg(&y[1]) * iy;
-        float thalf = j.frametime * ((float)(n / 2) + 0.5f) * (float)j.ave * it;
-        if (K == 3) { p[0] = y1; p[1] = thalf; p[2] = 0.f; }
-        else {
-            float t10 = j.frametime * ((float)(n / 10) + 0.5f) * (float)j.ave * it;
-            p[0] = y1 / 2; p[1] = t10; p[2] = y1 / 2; p[3] = thalf; p[4] = 0.f;
+        // reference initial guesses (java:10862-10864, 10917-10921) in f0, s, k
+        const double y1 = (double)__ldg(&y[1]) * (double)iy;
+        const double thalf = ((double)(n / 2) + 0.5) * (double)dts;
+        if (K == 3) {
+            p[0] = y1; p[1] = y1 / thalf; p[2] = 1.0 / thalf;
+        } else {
+            const double t10 = ((double)(n / 10) + 0.5) * (double)dts;
+            p[0] = y1; p[1] = 0.5 * y1 / t10; p[2] = 1.0 / t10; p[3] = 0.5 * y1 / thalf; p[4] = 1.0 / thalf;
         }
     }
     float A[K * K], g[K], lambda = 1e-3f;
-    double chi2 = exp_normal<K>(y, n, j.frametime, j.ave, iy, it, p, A, g, lane);
-    bool ok = isfinite(chi2);
-    for (int it_n = 0; ok && it_n < 300; it_n++) {
-        float h[K], pn[K];
-        // converged when the undamped Gauss-Newton step is negligible
-        if (solve_scaled_k<K>(A, g, 0.f, h)) {
+    bool precise = false;
+    double chi2 = exp_normal<K>(y, n, dts, iy, p, precise, A, g, lane);
+    const bool ok = isfinite(chi2);
+    int nprec = 0;
+    for (int it_n = 0; ok && it_n < 400; it_n++) {
+        unsigned fix;
+        float h[K];
+        if (exp_gn_step<K>(A, g, p, fix, h)) {
             bool conv = true;
-            for (int a = 0; a < K; a++) conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(p[a]) + 1e-7f;
-            if (conv) break;
+            for (int a = 0; a < K; a++) {
+                if ((fix >> a) & 1) continue;
+                const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
+                conv = conv && fabsf(h[a]) <= (precise ? 1e-7f : 1e-6f) * (float)fabs(p[a]) +
+                                                  (precise ? 1e-5f : 1e-4f) * sig;
+            }
+            if (conv) {
+                if (precise) break;
+                precise = true;
+                chi2 = exp_normal<K>(y, n, dts, iy, p, true, A, g, lane);
+                lambda = 1e-3f;
+                continue;
+            }
         }
-        if (!solve_scaled_k<K>(A, g, lambda, h)) { lambda *= 10.f; if (lambda > 1e20f) break; continue; }
-        for (int a = 0; a < K; a++) pn[a] = p[a] + h[a];
-        float An[K * K], gn[K];
-        double c2n = exp_normal<K>(y, n, j.frametime, j.ave, iy, it, pn, An, gn, lane);
-        if (isfinite(c2n) && c2n < chi2) {
-            for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
-            for (int a = 0; a < K * K; a++) A[a] = An[a];
-            chi2 = c2n;
-            lambda = fmaxf(lambda * 0.1f, 1e-12f);
-        } else {
+        bool stalled = false;
+        if (!solve_scaled_k<K>(A, g, lambda, fix, h)) {
             lambda *= 10.f;
-            if (lambda > 1e12f) break;
+            stalled = lambda > 1e10f;
+        } else {
+            double pn[K];
+            for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
+            for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
+            float An[K * K], gn[K];
+            const double c2n = exp_normal<K>(y, n, dts, iy, pn, precise, An, gn, lane);
+            if (isfinite(c2n) && c2n < chi2) {
+                for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
+                for (int a = 0; a < K * K; a++) A[a] = An[a];
+                chi2 = c2n;
+                lambda = fmaxf(lambda * 0.1f, 1e-12f);
+            } else {
+                lambda *= 10.f;
+                stalled = lambda > 1e10f;
+            }
         }
+        if (stalled) {
+            if (precise) break;
+            precise = true;
+            chi2 = exp_normal<K>(y, n, dts, iy, p, true, A, g, lane);
+            lambda = 1e-3f;
+        }
+        if (precise && ++nprec > 60) break;
     }
-    // back to data units
-    float res[5];
-    if (K == 3) { res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym; }
-    else {
-        res[0] = p[0] * ym; res[1] = p[1] * tmax; res[2] = p[2] * ym;
-        res[3] = p[3] * tmax; res[4] = p[4] * ym;
+    // back to data units: y = y_s / iy, t = t_s tmax
+    const double st = (double)dts / dt_pt;            // 1 / tmax
+    const double f0d = p[0] / (double)iy;
+    double sd[NC], kd[NC];
+    bool valid = ok && isfinite(f0d);
+    for (int c = 0; c < NC; c++) {
+        sd[c] = p[1 + 2 * c] * st / (double)iy;
+        kd[c] = p[2 + 2 * c] * st;
+        valid = valid && isfinite(sd[c]) && isfinite(kd[c]) && sd[c] != 0.0;  // java:9689, 9714
     }
-    bool valid = ok;
-    for (int a = 0; a < K; a++) valid = valid && isfinite(res[a]);
-    // java:9689 / 9714: correction applied only when the product is nonzero
-    if (K == 3) valid = valid && (res[0] * res[1] != 0.f);
-    else valid = valid && (res[0] * res[1] * res[2] * res[3] != 0.f);
-    float f0 = (K == 3) ? res[0] + res[2] : res[0] + res[2] + res[4];
-    float inv_f0 = 1.f / f0;
-    float bpl[kBleachStride] = {0.f};
-    for (int a = 0; a < K; a++) bpl[a] = res[a];
-    bpl[5] = 1.f / res[1];
-    if (K == 5) bpl[6] = 1.f / res[3];
+    // curve evaluation form per component (exp form unless slow over the run)
+    const double t_end = (double)j.frametime * ((double)j.num + 2.0);
+    float bpl[kBleachStride];
+    for (int a = 0; a < kBleachStride; a++) bpl[a] = 0.f;
+    double cconst = f0d, csum_amp = 0.0;
+    int flags = 0;
+    for (int c = 0; c < NC; c++) {
+        const double amp = sd[c] / kd[c];               // A_c (inf when k_c = 0)
+        bpl[5 + c] = (float)kd[c];
+        if (kd[c] * t_end <= 0.5) {
+            flags |= 1 << c;
+            bpl[7 + c] = (float)sd[c];
+        } else {
+            bpl[7 + c] = (float)amp;
+            cconst -= amp;
+        }
+        csum_amp += amp;
+        // reference form: A_c, tau_c
+        bpl[2 * c] = (float)amp;
+        bpl[2 * c + 1] = (float)(1.0 / kd[c]);
+    }
+    bpl[2 * NC] = (float)(f0d - csum_amp);               // C
+    bpl[13] = (float)cconst;
+    bpl[14] = (float)flags;
+    const float f0 = (float)f0d, inv_f0 = (float)(1.0 / f0d);
     float csum = 0.f;
     for (int x = lane; x < n; x += 32) {
         float yx = __ldg(&y[x]);
@@ -289,9 +425,7 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     csum = warp_sum(csum);
     if (lane == 0) {
         float *bp = bp_out + (size_t)tr * kBleachStride;
-        for (int a = 0; a < K; a++) bp[a] = res[a];
-        bp[5] = bpl[5];
-        bp[6] = bpl[6];
+        for (int a = 0; a < kBleachStride; a++) bp[a] = bpl[a];
         bp[9] = f0;
         bp[10] = inv_f0;
         bp[11] = valid ? 1.f : 0.f;

@@ -316,7 +316,6 @@ extern "C" int imfcs_fit(int n_fits, int n_points, const float *data, const floa
         set_error("unsupported model id");
         return -1;
     }
-    if (n_points > 160) { set_error("too many points per fit (max 160)"); return -1; }
     if (!user_info || user_info_size < (size_t)n_points * sizeof(float)) {
         set_error("user_info must hold n_points float abscissae");
         return -1;
