@@ -47,7 +47,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=0, help="pixels in the CPU baseline sample (0: auto)")
-    return ap.parse_args()
+    ap.add_argument("--frames", type=int, default=50000,
+                    help="frames of the stack (50000 is the benchmark; fewer only for profiling captures)")
+    a = ap.parse_args()
+    global T
+    T = a.frames
+    return a
 
 
 def dist_env():
@@ -157,19 +162,13 @@ def reference_arm(args):
     import oracle
     oracle.build()
     threads = os.cpu_count() or 1
-    from imaging_fcs_1_52_gb300 import engine, _lib  # config + synthetic data only
+    from imaging_fcs_1_52_gb300 import engine, _lib  # configuration only
+    from tests.synth import brownian_stack
     cfg = make_config(engine, _lib)
-    stack_np = None
-    try:
-        import torch
-        if torch.cuda.is_available():
-            stack_np = engine.to_numpy_u16(simulate_stack(engine, seed=1)[:, :8, :].contiguous())
-    except Exception:
-        stack_np = None
-    if stack_np is None:
-        from tests.synth import brownian_stack
-        stack_np = brownian_stack(W, 8, T, seed=1, tau_bleach=20.0)
-    sample = args.cpu_sample or 128
+    sample = args.cpu_sample or 1024
+    # the same simulation model and parameters on the host (numpy), one band
+    # of `sample` pixels x all frames
+    stack_np = brownian_stack(min(sample, W), max(1, sample // W), T, seed=1, tau_bleach=20.0)
     vals = []
     for i in range(args.warmup + args.steps):
         v, n, dt = cpu_baseline(stack_np, cfg, sample, threads)
@@ -179,10 +178,10 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sample / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "128x128x50000 uint16, single-exp bleach, P=16 Q=8, "
-                                            "OLS LM TIRF fit", "sample": f"{sample} pixels x 50000 frames"},
+            "data": "synthetic", "config": {"workload": f"128x128x{T} uint16, single-exp bleach, P=16 Q=8, "
+                                            "OLS LM TIRF fit", "sample": f"{sample} pixels x {T} frames"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{sample} pixels x 50000 frames, FP64 C restatement of the Java CPU path"},
+                             "sample": f"{sample} pixels x {T} frames, FP64 C restatement of the Java CPU path"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -218,12 +217,14 @@ def main():
         plan.execute(stack, out)
     barrier()
     corr_ms = []
+    launches = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         e0.record(stream)
         stage_acc = None
         for _ in range(args.steps):
             plan.execute(stack, out)
+            launches += plan.kernel_launches()
             torch.cuda.synchronize()     # stage events of this step are then readable
             st = plan.stage_times()
             corr_ms.append(st["correlator"])
@@ -268,29 +269,33 @@ def main():
         # ACF and blocked variance out (8 B each per pixel and channel)
         alg_bytes = T * H * W * 2 + cfg.npix * cfg.chanum * 8 * 2
         achieved = alg_bytes / (corr_avg * 1e-3) / 1e9
-        sample = args.cpu_sample or 64
-        stack_np = engine.to_numpy_u16(stack[:, :1, :].contiguous())
+        sample = args.cpu_sample or 4096
+        stack_np = engine.to_numpy_u16(stack[:, :max(1, sample // W), :].contiguous())
         cpu_v, cpu_n, cpu_dt = cpu_baseline(stack_np, cfg, sample, os.cpu_count() or 1)
+        # single-threaded, as the plugin's one worker thread runs it
+        cpu1_v, cpu1_n, cpu1_dt = cpu_baseline(stack_np, cfg, min(sample, 256), 1)
         fitted = int(out["fitted"].sum().item())
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU Monte-Carlo, seeded)",
-            "config": {"workload": "128x128x50000 uint16 stack; single-exp bleach; P=16 Q=8 (73 ch); "
+            "config": {"workload": f"128x128x{T} uint16 stack; single-exp bleach; P=16 Q=8 (73 ch); "
                                    "blocked variance; OLS LM TIRF fit (N, D, G)",
-                       "pixels_per_rank": cfg.npix, "frames": T, "l2": "inputs 1.64 GB > L2, no flush needed",
+                       "pixels_per_rank": cfg.npix, "frames": T, "l2": f"stack {T * H * W * 2 / 1e9:.2f} GB > L2 (129 MB), no flush needed",
                        "parallelism": f"pixel shards x{world}", "fitted_pixels": fitted},
             "e2e": {"value": world * cfg.npix / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "gpu_launches": 12 * args.steps,
+            "gpu_launches": launches,
             "stages_ms": {k: v / args.steps for k, v in stage_acc.items()},
             "roofline": {"kernel": "corr_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": load_profile_traffic(),
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": corr_avg},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                             "sample": f"{cpu_n} pixels x 50000 frames of the same stack, FP64 C oracle, "
+                             "sample": f"{cpu_n} pixels x {T} frames of the same stack, FP64 C oracle, "
                                        f"{cpu_dt:.1f} s"},
+            "cpu_baseline_single_thread": {"value": cpu1_v, "unit": UNIT, "cores": 1, "kind": "port",
+                                           "sample": f"{cpu1_n} pixels x {T} frames, {cpu1_dt:.1f} s"},
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

@@ -27,7 +27,7 @@ EXPORTS = [
     "imfcs_is_acf_memory_sufficient", "imfcs_calc_acf", "imfcs_fit", "imfcs_chanum",
     "imfcs_plan_create", "imfcs_plan_destroy", "imfcs_plan_scratch_bytes", "imfcs_plan_execute",
     "imfcs_plan_execute_host", "imfcs_diffusion_law", "imfcs_simulate", "imfcs_plan_bleach_params",
-    "imfcs_plan_set_timing", "imfcs_plan_stage_times",
+    "imfcs_plan_set_timing", "imfcs_plan_stage_times", "imfcs_plan_kernel_launches",
 ]
 
 
@@ -111,6 +111,7 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_plan_bleach_params.argtypes = [vp, vp, C.c_int]
     L.imfcs_plan_set_timing.argtypes = [vp, C.c_int]
     L.imfcs_plan_stage_times.argtypes = [vp, vp, C.c_int]
+    L.imfcs_plan_kernel_launches.argtypes = [vp]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

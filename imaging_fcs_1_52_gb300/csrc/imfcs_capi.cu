@@ -227,6 +227,7 @@ struct imfcs_plan {
     int chanum = 0, npix = 0, nseg = 0, nbseg = 0, pnum_max = 0, nfitpts = 0, k = 0;
     int idx[IMFCS_NPARAM];
     int num_sms = 1;
+    int launches = 0;                 // kernels launched by the last execute
     double uscale = 1, uoff = 0;
     bool given_bleach = false;
     std::vector<DevBuf> bufs;
@@ -526,6 +527,7 @@ static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const floa
     a.out_iter = iters ? iters : pl->fit_iter;
     a.out_hess = pl->fit_hess;
     CK(launch_lm(a, pl->num_sms, s));
+    pl->launches += 1;
     EpilogueArgs e;
     memset(&e, 0, sizeof(e));
     e.npix = pl->npix;
@@ -551,6 +553,7 @@ static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const floa
     e.mc = a.mc;
     e.lagtime = pl->lagtime;
     CK(launch_fit_epilogue(e, s));
+    pl->launches += 1;
     return 0;
 }
 
@@ -565,20 +568,25 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     double *acf = dev_out->acf ? dev_out->acf : pl->acf_int;
     double *var = dev_out->var ? dev_out->var : pl->var_int;
     for (int i = 0; i <= imfcs_plan::kStages; i++) pl->ev_used[i] = false;
+    pl->launches = 0;
     pl->mark(0, s);
     CK(launch_trace(j, dev_stack, pl->trace, s));
     if (pl->given_bleach) CK(launch_center_given(j, pl->trace, pl->bparams, s));
     else CK(launch_bleach(j, pl->trace, pl->proj, (float)pl->uscale, (float)pl->uoff, pl->bparams, s));
+    pl->launches += 2;
     pl->mark(1, s);
     CK(launch_monitor(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->snap_pos, pl->nseg,
                       pl->segtot, pl->snap_part, pl->mon, pl->blkmon, s));
+    pl->launches += 2;
     pl->mark(2, s);
     CK(launch_block(j, dev_stack, pl->bparams, pl->basis, pl->blkmon, pl->nbseg, pl->s1, pl->s2,
                     pl->segsum, pl->blk_ind, pl->blk_ok, s));
+    pl->launches += 2;
     pl->mark(3, s);
     CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->mon, pl->blk_ind, acf, var,
                    dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats,
                    c.gls, pl->dev_err, s));
+    pl->launches += 1;
     if (dev_out->blocked_ind) CK(cudaMemcpyAsync(dev_out->blocked_ind, pl->blk_ind, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     if (dev_out->blocked_ok) CK(cudaMemcpyAsync(dev_out->blocked_ok, pl->blk_ok, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     pl->mark(4, s);
@@ -597,12 +605,16 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
         g.ok = pl->gls_ok;
         g.covmats_out = dev_out->covmats;
         CK(launch_gls(g, s));
+        pl->launches += 1;
     }
     pl->mark(5, s);
     if (c.do_fit || c.bayes) {
         const float *y = c.gls ? pl->ytrans : pl->fit_y;
         const float *w = c.gls ? nullptr : pl->fit_w;
-        if (!c.gls) CK(launch_ols_prepare(pl->npix, chanum, c.fitstart, pl->nfitpts, acf, var, pl->fit_y, pl->fit_w, s));
+        if (!c.gls) {
+            CK(launch_ols_prepare(pl->npix, chanum, c.fitstart, pl->nfitpts, acf, var, pl->fit_y, pl->fit_w, s));
+            pl->launches += 1;
+        }
         if (c.do_fit) {
             if (!dev_out->fitres) { set_error("fitres output required when do_fit is set"); return 1; }
             if (run_fit(pl, s, acf, y, w, pl->fit_init, pl->k, pl->idx, dev_out->fitres, dev_out->chi2,
@@ -617,7 +629,10 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
             if (run_fit(pl, s, acf, y, w, pl->bfit_init2, 5, i2, pl->bfit_res, nullptr, nullptr, nullptr,
                         pl->logp2, pl->fit_par))
                 return 1;
-            if (dev_out->bayes_prob) CK(launch_bayes_combine(pl->npix, pl->logp1, pl->logp2, dev_out->bayes_prob, s));
+            if (dev_out->bayes_prob) {
+                CK(launch_bayes_combine(pl->npix, pl->logp1, pl->logp2, dev_out->bayes_prob, s));
+                pl->launches += 1;
+            }
         }
     }
     pl->mark(6, s);
@@ -822,6 +837,12 @@ extern "C" int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out,
     cudaError_t e = cudaMemcpy(host_out, plan->bparams, sizeof(float) * kBleachStride * n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { set_error(cuda_msg(e, "bleach params")); return -1; }
     return n;
+}
+
+extern "C" int imfcs_plan_kernel_launches(const imfcs_plan *plan)
+{
+    if (!plan) { set_error("null plan"); return -1; }
+    return plan->launches;
 }
 
 extern "C" int imfcs_plan_set_timing(imfcs_plan *plan, int enable)

@@ -179,6 +179,13 @@ class Plan:
             raise _lib.ImfcsError(_lib.last_error())
         return {k: float(ms[i]) for i, k in enumerate(self.STAGES)}
 
+    def kernel_launches(self) -> int:
+        """CUDA kernels launched by the last execution."""
+        n = self._L.imfcs_plan_kernel_launches(self._h)
+        if n < 0:
+            raise _lib.ImfcsError(_lib.last_error())
+        return int(n)
+
     def bleach_params(self) -> np.ndarray:
         """Per-trace bleach parameters of the last execution (diagnostic)."""
         n = self.cfg.npix * (2 if (self.cfg.cfx or self.cfg.cfy) else 1)

@@ -206,9 +206,14 @@ IMFCS_API size_t imfcs_plan_scratch_bytes(const imfcs_plan *plan);
 
 /* Diagnostic (no counterpart in the reference): copies the per-trace bleach
  * parameters of the last execution to host memory, 16 floats per trace
- * ([0..8] fit coefficients, [9] f0, [11] valid flag, [12] centre).  Returns
- * the number of traces. */
+ * ([0..8] polynomial coefficients, or A, tau, C / A1, tau1, A2, tau2, C of
+ * the exponential fit; [9] f0, [11] valid flag, [12] centre).  Returns the
+ * number of traces. */
 IMFCS_API int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out, int max_traces);
+
+/* Diagnostic (no counterpart in the reference): number of CUDA kernels the
+ * last imfcs_plan_execute / imfcs_plan_execute_host launched. */
+IMFCS_API int imfcs_plan_kernel_launches(const imfcs_plan *plan);
 
 /* Stage timing (no counterpart in the reference): when enabled, every
  * execution records CUDA events around its stages on the execution stream;
