@@ -28,6 +28,7 @@ EXPORTS = [
     "imfcs_plan_create", "imfcs_plan_destroy", "imfcs_plan_scratch_bytes", "imfcs_plan_execute",
     "imfcs_plan_execute_host", "imfcs_diffusion_law", "imfcs_simulate", "imfcs_plan_bleach_params",
     "imfcs_plan_set_timing", "imfcs_plan_stage_times", "imfcs_plan_kernel_launches",
+    "imfcs_fit_device_noalloc",
 ]
 
 
@@ -112,6 +113,8 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_plan_set_timing.argtypes = [vp, C.c_int]
     L.imfcs_plan_stage_times.argtypes = [vp, vp, C.c_int]
     L.imfcs_plan_kernel_launches.argtypes = [vp]
+    L.imfcs_fit_device_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int, vp, C.c_float, C.c_int, C.c_int,
+                                           vp, vp, vp, vp, vp, vp, vp]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

@@ -149,6 +149,29 @@ IMFCS_API int imfcs_fit(int n_fits, int n_points, const float *data, const float
               float *output_parameters, int *output_states, float *output_chi_squares,
               int *output_n_iterations);
 
+/* No counterpart in the reference.  The same fit as imfcs_fit on DEVICE
+ * buffers, asynchronous on `stream`, and without any device allocation: for
+ * callers that cannot allocate at fit time -- a host pipeline that keeps other
+ * streams busy (cudaMalloc/cudaFree synchronise the device and would stall
+ * them), or one whose device memory is fully reserved by its own pool.
+ * data/weights [n_fits][n_points], initial_parameters and output_parameters
+ * [n_fits][20 (ACF_1D) or 11 (LINEAR_1D)], user_info = n_points float
+ * abscissae, outputs (states, chi-squares, iterations: each nullable) are
+ * device pointers; parameters_to_fit is a host array.  Scratch is a fixed
+ * file-scope device array sized for IMFCS_FIT_NOALLOC_MAX_FITS fits (2 MB);
+ * larger batches are rejected with an error (split them).  No part of the
+ * scratch needs to start at zero: each call writes every element it reads.
+ * The first call on a device resolves the scratch address
+ * (cudaGetSymbolAddress) and should precede any stream capture.  Calls that
+ * overlap on one device (other host threads or streams) share the scratch
+ * and race: serialise them.  Returns 0 / -1 (imfcs_get_last_error). */
+#define IMFCS_FIT_NOALLOC_MAX_FITS 16384
+IMFCS_API int imfcs_fit_device_noalloc(int n_fits, int n_points, const float *data, const float *weights,
+              int model_id, const float *initial_parameters, float tolerance,
+              int max_n_iterations, int num_valid_coefs, const int *parameters_to_fit,
+              const float *user_info, float *output_parameters, int *output_states,
+              float *output_chi_squares, int *output_n_iterations, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* GB300-native whole-path API (uint16 stack -> ACF, variance, fits).        */
 /* ------------------------------------------------------------------------ */
