@@ -240,7 +240,7 @@ struct imfcs_plan {
     float4 *mon = nullptr, *blkmon = nullptr;
     float *s1 = nullptr, *s2 = nullptr, *segsum = nullptr;
     int *blk_ind = nullptr, *blk_ok = nullptr;
-    float *stats = nullptr, *bprod = nullptr;
+    float *stats = nullptr, *bprod = nullptr, *streams = nullptr;
     float *linv = nullptr, *ytrans = nullptr;
     int *gls_ok = nullptr;
     float *fit_y = nullptr, *fit_w = nullptr, *fit_x = nullptr, *fit_x_gls = nullptr;
@@ -399,7 +399,8 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     AL(pl->segsum, np * pl->nbseg);
     AL(pl->blk_ind, np);
     AL(pl->blk_ok, np);
-    AL(pl->stats, (size_t)chanum * 5 * np);
+    AL(pl->stats, corr_stats_floats(j));
+    AL(pl->streams, corr_stream_floats(j));
     AL(pl->acf_int, np * chanum);
     AL(pl->var_int, np * chanum);
     AL(pl->lagtime, chanum);
@@ -584,9 +585,9 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     pl->launches += 2;
     pl->mark(3, s);
     CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->mon, pl->blk_ind, acf, var,
-                   dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats,
+                   dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats, pl->streams,
                    c.gls, pl->dev_err, s));
-    pl->launches += 1;
+    pl->launches += corr_kernel_count(j);
     if (dev_out->blocked_ind) CK(cudaMemcpyAsync(dev_out->blocked_ind, pl->blk_ind, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     if (dev_out->blocked_ok) CK(cudaMemcpyAsync(dev_out->blocked_ok, pl->blk_ok, sizeof(int) * pl->npix, cudaMemcpyDeviceToDevice, s));
     pl->mark(4, s);

@@ -28,27 +28,11 @@
 #include <stdint.h>
 #include <string.h>
 
-#include "imfcs_internal.cuh"
+#include "imfcs_corr.cuh"
 
 namespace imfcs {
 
 constexpr int kCorrThreads = 128;
-constexpr int kStatN = 5;   // per-lag block statistics: Ahi, Alo, S1, S2, r
-
-struct CorrOut {
-    double *acf, *var, *sd;
-    double *nb_mean, *nb_cov;
-    float *bprod;        // GLS: [pix][chanum-1][pnum_max]
-    int pnum_stride;
-    float *stats;        // scratch [chanum][kStatN][npix]
-    int gls;
-    int *err;            // set to 1 when a bounded wait gave up
-};
-
-__device__ __forceinline__ float &stat_ref(float *stats, int npix, int lag, int s, int pix)
-{
-    return stats[((size_t)lag * kStatN + s) * npix + pix];
-}
 
 // Block end for the lags [lagbase, lagbase+nl) of one level (out of line:
 // it runs once per 2^(ind-k) direct samples).  acc: the lags' block sums of
@@ -592,8 +576,15 @@ template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, c
                                            const __grid_constant__ CUtensorMap);
 
 // ---------------------------------------------------------------------------
-// Host side: shared memory size, TMA geometry and tensor map, launch.
+// Host side: shared memory size, TMA geometry and tensor map, launch.  Jobs
+// with Q >= 5 run the per-pixel kernel of imfcs_corr2.cu; this CTA-tiled
+// kernel covers the rest (blocks shorter than 16 samples).
 // ---------------------------------------------------------------------------
+bool corr2_supported(const Job &j);
+cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
+                         const float *basis, const float4 *mon, const int *blk_ind, const CorrOut &o,
+                         float *streams, cudaStream_t stream);
+
 size_t corr_smem_bytes(int q, bool ccf) { return corr_smem_floats_dev(q, ccf) * sizeof(float); }
 
 // TMA box over the raw stack that covers every window of a 32-pixel row
@@ -641,11 +632,13 @@ static bool encode_stack_map(const Job &j, const void *stack, const TmaGeom &g, 
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
                         const float *basis, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
-                        int pnum_stride, float *stats, int gls, int *err, cudaStream_t stream)
+                        int pnum_stride, float *stats, float *streams, int gls, int *err,
+                        cudaStream_t stream)
 {
     CorrOut o;
     o.acf = acf; o.var = var; o.sd = sd; o.nb_mean = nb_mean; o.nb_cov = nb_cov;
     o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls; o.err = err;
+    if (corr2_supported(j)) return launch_corr2(j, li, stack, bparams, basis, mon, blk_ind, o, streams, stream);
     TmaGeom g = tma_geometry(j, stack);
     CUtensorMap map;
     memset(&map, 0, sizeof(map));

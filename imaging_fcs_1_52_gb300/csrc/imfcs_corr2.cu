@@ -1,0 +1,685 @@
+// imfcs_corr2.cu -- multi-tau correlator with blocked variance as a chain of
+// streaming kernels, no block-wide synchronisation.
+//
+// Restates calculateCF (Imaging_FCS_1_52.java:9425-9648) with the same
+// per-lag block statistics and outputs as corr_kernel:
+//
+//   values    the binned, background-subtracted, bleach-corrected and
+//             centred value of every (trace, frame) is written once as FP32,
+//             frame-major ([t][pixel]): the level-0 sample stream s0;
+//   pair k    one thread per (pixel, frame segment) streams the level-k
+//             samples and correlates levels k and k+1 (lags 0..16 at level 0,
+//             delays 9..16 above) in registers: rings of the last 32 samples
+//             whose positions are compile-time constants inside a 64-sample
+//             unrolled step; it writes the level-(k+2) samples (pair sums of
+//             its level-(k+1) samples) for the next kernel;
+//   tail      levels k0..Q-1 whose blocks may be shorter than 16 samples, one
+//             sample at a time with rings in shared memory;
+//   finalise  per (pixel, lag): segments combined in FP64, outputs.
+//
+// Products are grouped by their direct sample y (processed when the delayed
+// samples y..y+16 are present), so the blocks of the blocked variance
+// (2^(ind-k) products, java:9502-9511) end at the same y for every lag of a
+// level.  With the window means a, b of the centred samples from the monitor
+// pass, the blocked product of block z is
+//   P_z = (A_z - b B_z - a D_z + L a b) / L
+// (A_z: sum of products, B_z: sum of direct samples, D_z: sum of the delayed
+// samples y+d over the block, from the block's running sum and the "heads",
+// the sums of the first d delayed samples of a block).  Frame segments are
+// multiples of every pixel's block length (2^ind frames), so no block spans
+// two threads; each segment keeps its own statistics.
+#include "imfcs_corr.cuh"
+
+namespace imfcs {
+
+constexpr int kC2Threads = 64;
+constexpr int kVFrames = 256;                // frames per thread in the values pass
+constexpr int kRing = 17;                    // tail rings: samples n-16..n
+constexpr int kTailFieldsAcf = kRing + 8 + 2 + 8 + 2;      // ring, acc, b0, b1, head, pend0, n
+constexpr int kTailFieldsCcf = kTailFieldsAcf + kRing + 1;  // + delayed ring, pend1
+constexpr int kHeadFields = (kP + 1) + 8;                   // first-level heads d = 0..16, second-level d = 9..16
+
+// Arguments shared by the pair, tail and finalise kernels.
+struct C2Args {
+    CorrOut o;
+    const float4 *mon;        // [pix][chanum] (a, b, dm, Dm)
+    const int *blk_ind;       // [pix]
+    const LagInfo *li;
+    int npix, chanum, q, num;
+    int numbin[kMaxLevels];
+    int seg_log[kMaxLevels];  // frame segment (log2) of the kernel owning each level
+    size_t stat_stride;       // floats per segment in o.stats
+};
+
+// Per-thread context.
+struct C2Ctx {
+    float *stats;             // this segment's statistics
+    const float4 *mon;        // this pixel's monitors
+    float *bprod;
+    int npix, pix, chanum, pnum_stride, gls;
+    int ind, pnum, zfirst;
+};
+
+// One block end of one lag: total, blocked product and its statistics.
+__device__ __forceinline__ void c2_block_stat(const C2Ctx &c, int lag, float A, float B0, float D, int L, int z)
+{
+    const float4 m = __ldg(&c.mon[lag]);
+    const float a = m.x, b = m.y;
+    const float P = (A - b * B0 - a * D + (float)L * a * b) / (float)L;
+    float &ahi = stat_ref(c.stats, c.npix, lag, 0, c.pix);
+    float &alo = stat_ref(c.stats, c.npix, lag, 1, c.pix);
+    ff t = {ahi, alo};
+    ff_add(t, A);
+    ahi = t.hi;
+    alo = t.lo;
+    if (z < c.pnum) {
+        float &r = stat_ref(c.stats, c.npix, lag, 4, c.pix);
+        if (z == c.zfirst) r = P;      // per-segment shift of the block statistics
+        const float dv = P - r;
+        stat_ref(c.stats, c.npix, lag, 2, c.pix) += dv;
+        stat_ref(c.stats, c.npix, lag, 3, c.pix) += dv * dv;
+        if (c.gls && lag >= 1) c.bprod[((size_t)c.pix * (c.chanum - 1) + (lag - 1)) * c.pnum_stride + z] = P;
+    }
+}
+
+__device__ __forceinline__ void c2_add_total(const C2Ctx &c, int lag, float A)
+{
+    float &ahi = stat_ref(c.stats, c.npix, lag, 0, c.pix);
+    float &alo = stat_ref(c.stats, c.npix, lag, 1, c.pix);
+    ff t = {ahi, alo};
+    ff_add(t, A);
+    ahi = t.hi;
+    alo = t.lo;
+}
+
+__device__ __forceinline__ void c2_ctx(C2Ctx &c, const C2Args &a, int pix, int seg, int k)
+{
+    c.stats = a.o.stats + (size_t)seg * a.stat_stride;
+    c.mon = a.mon + (size_t)pix * a.chanum;
+    c.bprod = a.o.bprod;
+    c.npix = a.npix;
+    c.pix = pix;
+    c.chanum = a.chanum;
+    c.pnum_stride = a.o.pnum_stride;
+    c.gls = a.o.gls;
+    c.ind = a.blk_ind[pix];
+    c.pnum = a.li->pnum_by_ind[c.ind];
+    c.zfirst = (seg << a.seg_log[k]) >> c.ind;
+}
+
+// ---------------------------------------------------------------------------
+// Values pass: s0[t][pix] (direct trace A) and, for cross-correlation,
+// s0b[t][pix] (displaced trace B).
+// ---------------------------------------------------------------------------
+__global__ void c2_values_kernel(Job j, const void *stack, const float *bparams, const float *basis,
+                                 float *s0a, float *s0b)
+{
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= j.npix) return;
+    const int t0 = blockIdx.y * kVFrames, t1 = min(t0 + kVFrames, j.num);
+    for (int tr = 0; tr < (j.is_ccf ? 2 : 1); tr++) {
+        const int trace = tr ? j.npix + pix : pix;
+        int x0, y0;
+        trace_origin(j, trace, x0, y0);
+        float bp[kBleachStride];
+#pragma unroll
+        for (int i = 0; i < kBleachStride; i++) bp[i] = __ldg(&bparams[(size_t)trace * kBleachStride + i]);
+        const bool corr = j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f;
+        float *dst = tr ? s0b : s0a;
+        for (int t = t0; t < t1; t += 8) {
+            float v[8];
+            window_values<8>(j, stack, x0, y0, t, t1, v);
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int tt = t + u;
+                if (tt >= t1) break;
+                float x = v[u];
+                if (corr) {
+                    const float ft = frame_time(j, tt);
+                    x = bleach_correct(x, bleach_f(bp, j.bleach, j.poly_order, ft,
+                                                   basis ? basis + (size_t)tt * (j.poly_order + 1) : nullptr),
+                                       bp[9], bp[10]);
+                }
+                dst[(size_t)tt * j.npix + pix] = x - bp[12];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pair kernel: levels k (first) and k+1 (second) of one (pixel, segment).
+// FIRST17: the first level is level 0 (lags 0..16); otherwise its lags are
+// delays 9..16.  TWO: the second level exists (k+1 < Q).
+// ---------------------------------------------------------------------------
+template <bool FIRST17>
+struct PairReg {
+    static constexpr int NF = FIRST17 ? kP + 1 : 8;   // first-level lags
+    static constexpr int DF = FIRST17 ? 0 : 9;        // first-level delay of lag 0
+    float wB[32], wA[32];      // first-level rings (delayed / direct trace), index n & 31
+    float rB[32], rA[32];      // second-level rings, index n & 31
+    float accF[NF], accS[8];
+    float bF0, bF1, bS0, bS1;
+    float curB[16], curA[16];  // samples n .. n+15 in flight (slot n & 15)
+};
+
+struct PairGeo {
+    const float *inA, *inB;    // level-k samples [n][npix]
+    float *outA, *outB;        // level-(k+2) samples [n][npix] or nullptr
+    int k, nk, nk1, nk2;       // level and sample counts of levels k, k+1, k+2
+    int sk0, sk1;              // direct samples [sk0, sk1) of level k
+    int LF, LS;                // block lengths (samples) of levels k and k+1
+    int lagF, lagS;            // first lag index of the two levels
+};
+
+__device__ __forceinline__ float c2_load(const float *in, int n, int nk, int npix, int pix)
+{
+    return n < nk ? __ldg(&in[(size_t)n * npix + pix]) : 0.f;
+}
+
+template <bool CCF, bool FIRST17, bool TWO, int QP>
+__device__ __forceinline__ void c2_pair_group(const C2Ctx &c, const PairGeo &p, float *heads, int nt,
+                                              PairReg<FIRST17> &R, int g)
+{
+    constexpr int NF = PairReg<FIRST17>::NF, DF = PairReg<FIRST17>::DF;
+    constexpr int PH0 = 16 * (QP & 1);
+    constexpr int PH1 = 8 * QP;
+    const int n0 = 16 * g;
+    const bool dirF = (n0 - 16 >= p.sk0) && (n0 - 16 < p.sk1);          // direct samples n0-16 .. n0-1
+    const bool dirS = TWO && (n0 - 32 >= p.sk0) && (n0 - 32 < p.sk1);   // second-level 8g-16 .. 8g-9
+#pragma unroll
+    for (int jj = 0; jj < 16; jj++) {
+        const int n = n0 + jj;
+        const float vB = R.curB[jj];
+        R.curB[jj] = c2_load(p.inB, n + 16, p.nk, c.npix, c.pix);
+        R.wB[(PH0 + jj) & 31] = vB;
+        if (CCF) {
+            R.wA[(PH0 + jj) & 31] = R.curA[jj];
+            R.curA[jj] = c2_load(p.inA, n + 16, p.nk, c.npix, c.pix);
+        }
+        if (dirF) {
+            // direct sample y = n - 16 with delayed samples y + DF .. y + 16 = n
+            const float x0 = CCF ? R.wA[(PH0 + 16 + jj) & 31] : R.wB[(PH0 + 16 + jj) & 31];
+#pragma unroll
+            for (int d = 0; d < NF; d++) R.accF[d] = fmaf(x0, R.wB[(PH0 + 16 + jj + DF + d) & 31], R.accF[d]);
+            R.bF0 += x0;
+            R.bF1 += R.wB[(PH0 + 16 + jj) & 31];
+        }
+        if (TWO && (jj & 1)) {
+            // second-level sample m = 8g + jj/2 from first-level samples n-1, n
+            const int i1 = jj >> 1;
+            const int m = 8 * g + i1;
+            const bool ok = m < p.nk1;
+            const float sB = ok ? R.wB[(PH0 + jj - 1) & 31] + R.wB[(PH0 + jj) & 31] : 0.f;
+            R.rB[(PH1 + i1) & 31] = sB;
+            if (CCF) R.rA[(PH1 + i1) & 31] = ok ? R.wA[(PH0 + jj - 1) & 31] + R.wA[(PH0 + jj) & 31] : 0.f;
+            if (dirS) {
+                // direct sample y1 = m - 16, delayed samples y1 + 9 .. y1 + 16 = m
+                const float x1 = CCF ? R.rA[(PH1 + i1 + 16) & 31] : R.rB[(PH1 + i1 + 16) & 31];
+#pragma unroll
+                for (int l = 0; l < 8; l++) R.accS[l] = fmaf(x1, R.rB[(PH1 + i1 + 16 + 9 + l) & 31], R.accS[l]);
+                R.bS0 += x1;
+                R.bS1 += R.rB[(PH1 + i1 + 16) & 31];
+            }
+        }
+    }
+    // level-(k+2) samples 4g .. 4g+3 from second-level samples 8g .. 8g+7
+    if (TWO && p.outB) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int m2 = 4 * g + i;
+            if (m2 >= (p.sk0 >> 2) && m2 < (p.sk1 >> 2) && m2 < p.nk2) {
+                p.outB[(size_t)m2 * c.npix + c.pix] = R.rB[(PH1 + 2 * i) & 31] + R.rB[(PH1 + 2 * i + 1) & 31];
+                if (CCF)
+                    p.outA[(size_t)m2 * c.npix + c.pix] = R.rA[(PH1 + 2 * i) & 31] + R.rA[(PH1 + 2 * i + 1) & 31];
+            }
+        }
+    }
+    // heads of the segment's first blocks (its first 16 samples of either
+    // level sit at ring positions 0..15)
+    if (QP == 1 && n0 == p.sk0 + 16) {
+        float h = 0.f;
+        heads[0] = 0.f;
+#pragma unroll
+        for (int d = 1; d <= kP; d++) { h += R.wB[(d - 1) & 31]; heads[d * nt] = h; }
+    }
+    if (TWO && QP == 2 && n0 == p.sk0 + 32) {
+        float h = 0.f;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            h += R.rB[i & 31];
+            if (i + 1 >= 9) heads[(kP + 1 + i + 1 - 9) * nt] = h;
+        }
+    }
+    // first-level block end: last direct sample y = n0 - 1; heads of the next
+    // block are samples n0 .. n0 + d - 1 (this group)
+    if (dirF && (n0 & (p.LF - 1)) == 0) {
+        const int z = n0 / p.LF - 1;
+#pragma unroll 1
+        for (int l = 0; l < NF; l++) {
+            const int d = DF + l;
+            float nh = 0.f;
+#pragma unroll
+            for (int i = 0; i < kP; i++)
+                if (i < d) nh += R.wB[(PH0 + i) & 31];
+            float A = 0.f;
+#pragma unroll
+            for (int ll = 0; ll < NF; ll++)
+                if (ll == l) A = R.accF[ll];
+            float *hd = heads + d * nt;
+            c2_block_stat(c, p.lagF + l, A, R.bF0, R.bF1 - hd[0] + nh, p.LF, z);
+            hd[0] = nh;
+        }
+#pragma unroll
+        for (int l = 0; l < NF; l++) R.accF[l] = 0.f;
+        R.bF0 = 0.f;
+        R.bF1 = 0.f;
+    }
+    // second-level block end: last direct sample y1 = 8g - 9; heads of the
+    // next block are second-level samples 8g - 8 .. 8g - 9 + d
+    if (dirS && ((8 * g - 8) & (p.LS - 1)) == 0) {
+        const int z = (8 * g - 8) / p.LS - 1;
+#pragma unroll 1
+        for (int l = 0; l < 8; l++) {
+            const int d = 9 + l;
+            float nh = 0.f;
+#pragma unroll
+            for (int i = 1; i <= kP; i++)
+                if (i <= d) nh += R.rB[(PH1 - 9 + i + 32) & 31];
+            float A = 0.f;
+#pragma unroll
+            for (int ll = 0; ll < 8; ll++)
+                if (ll == l) A = R.accS[ll];
+            float *hd = heads + (kP + 1 + l) * nt;
+            c2_block_stat(c, p.lagS + l, A, R.bS0, R.bS1 - hd[0] + nh, p.LS, z);
+            hd[0] = nh;
+        }
+#pragma unroll
+        for (int l = 0; l < 8; l++) R.accS[l] = 0.f;
+        R.bS0 = 0.f;
+        R.bS1 = 0.f;
+    }
+}
+
+template <bool CCF, bool FIRST17, bool TWO>
+__global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const float *inA, const float *inB,
+                                                             float *outA, float *outB, int k)
+{
+    __shared__ float heads_sm[kHeadFields * kC2Threads];
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
+    if (pix >= a.npix) return;          // no block-wide synchronisation below
+    float *heads = heads_sm + tid;
+    C2Ctx c;
+    c2_ctx(c, a, pix, seg, k);
+    PairGeo p;
+    p.inA = CCF ? inA : inB;
+    p.inB = inB;
+    p.outA = outA;
+    p.outB = outB;
+    p.k = k;
+    p.nk = a.numbin[k];
+    p.nk1 = TWO ? a.numbin[k + 1] : 0;
+    p.nk2 = (TWO && k + 2 < a.q) ? a.numbin[k + 2] : 0;
+    const int s0 = seg << a.seg_log[k];
+    const int s1 = s0 + (1 << a.seg_log[k]);
+    if (s0 >= a.num) return;
+    p.sk0 = s0 >> k;
+    p.sk1 = s1 >= a.num ? p.nk : (s1 >> k);
+    p.LF = 1 << (c.ind - k);
+    p.LS = 1 << (c.ind - k - 1);
+    p.lagF = FIRST17 ? 0 : (kP + 1) + (k - 1) * 8;
+    p.lagS = (kP + 1) + k * 8;
+
+    for (int lag = p.lagF; lag < p.lagF + PairReg<FIRST17>::NF; lag++)
+        for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
+    if (TWO)
+        for (int lag = p.lagS; lag < p.lagS + 8; lag++)
+            for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
+    for (int f = 0; f < kHeadFields; f++) heads[f * nt] = 0.f;
+
+    PairReg<FIRST17> R;
+#pragma unroll
+    for (int i = 0; i < 32; i++) { R.wB[i] = 0.f; R.wA[i] = 0.f; R.rB[i] = 0.f; R.rA[i] = 0.f; }
+#pragma unroll
+    for (int d = 0; d < PairReg<FIRST17>::NF; d++) R.accF[d] = 0.f;
+#pragma unroll
+    for (int l = 0; l < 8; l++) R.accS[l] = 0.f;
+    R.bF0 = R.bF1 = R.bS0 = R.bS1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        R.curB[i] = c2_load(p.inB, p.sk0 + i, p.nk, c.npix, pix);
+        R.curA[i] = CCF ? c2_load(p.inA, p.sk0 + i, p.nk, c.npix, pix) : 0.f;
+    }
+    // groups of 16 samples: the segment's, then 48 more (the second level's
+    // last direct samples need 16 second-level samples past the segment)
+    const int g0 = p.sk0 / 16;
+    int ng = (p.sk1 - p.sk0 + 48 + 15) / 16;
+    ng = (ng + 3) & ~3;
+    for (int g = g0; g < g0 + ng; g += 4) {
+        c2_pair_group<CCF, FIRST17, TWO, 0>(c, p, heads, nt, R, g);
+        c2_pair_group<CCF, FIRST17, TWO, 1>(c, p, heads, nt, R, g + 1);
+        c2_pair_group<CCF, FIRST17, TWO, 2>(c, p, heads, nt, R, g + 2);
+        c2_pair_group<CCF, FIRST17, TWO, 3>(c, p, heads, nt, R, g + 3);
+    }
+    // the partial blocks at the end into the totals
+#pragma unroll
+    for (int l = 0; l < PairReg<FIRST17>::NF; l++) c2_add_total(c, p.lagF + l, R.accF[l]);
+    if (TWO)
+#pragma unroll
+        for (int l = 0; l < 8; l++) c2_add_total(c, p.lagS + l, R.accS[l]);
+}
+
+// ---------------------------------------------------------------------------
+// Tail kernel: levels k0..Q-1 of one (pixel, segment), one sample at a time.
+// State of level k at hs[((k - k0) * F + f) * nt].
+// ---------------------------------------------------------------------------
+template <bool CCF>
+__device__ __forceinline__ void c2_tail_push(const C2Ctx &c, const C2Args &a, float *hs, int nt, int k0, int k,
+                                             int kstop, int s0, int s1, float v0, float v1)
+{
+    constexpr int F = CCF ? kTailFieldsCcf : kTailFieldsAcf;
+    constexpr int RING0 = 0, ACC = kRing, B0 = ACC + 8, B1 = B0 + 1, HEAD = B1 + 1, PEND0 = HEAD + 8,
+                  NCNT = PEND0 + 1, RING1 = NCNT + 1, PEND1 = RING1 + kRing;
+    for (;;) {
+        float *s = hs + (size_t)(k - k0) * F * nt;
+#define HS(f) s[(f) * nt]
+        const int n = (int)HS(NCNT);
+        HS(NCNT) = (float)(n + 1);
+        if (n >= a.numbin[k]) { v0 = 0.f; v1 = 0.f; }
+        const int pos = n % kRing;
+        HS(RING0 + pos) = v0;
+        if (CCF) HS(RING1 + pos) = v1;
+        const int RD = CCF ? RING1 : RING0;      // delayed-trace ring
+        const int y = n - 16;
+        const int ys0 = s0 >> k, ys1 = (s1 >= a.num) ? a.numbin[k] : (s1 >> k);   // segment's direct samples
+        if (y >= ys0 && y < ys1) {
+            const int base = (pos + 1 == kRing) ? 0 : pos + 1;   // ring position of sample y
+            if (y == ys0) {
+                float h = 0.f;
+                for (int i = 0; i < 16; i++) {
+                    int q = base + i;
+                    q -= (q >= kRing) ? kRing : 0;
+                    h += HS(RD + q);
+                    if (i + 1 >= 9) HS(HEAD + i + 1 - 9) = h;
+                }
+            }
+            const float x0 = HS(RING0 + base);
+            float x1[8];
+#pragma unroll
+            for (int l = 0; l < 8; l++) {
+                int q = base + 9 + l;
+                q -= (q >= kRing) ? kRing : 0;
+                x1[l] = HS(RD + q);
+            }
+#pragma unroll
+            for (int l = 0; l < 8; l++) HS(ACC + l) = fmaf(x0, x1[l], HS(ACC + l));
+            HS(B0) += x0;
+            HS(B1) += HS(RD + base);
+            const int lk = c.ind - k;
+            const int L = lk > 0 ? (1 << lk) : 1;
+            if (((y + 1) & (L - 1)) == 0) {
+                // heads of the next block: sums of the delayed samples y+1 .. y+d
+                float nh[8], h = 0.f;
+#pragma unroll
+                for (int i = 1; i <= 16; i++) {
+                    int q = base + i;
+                    q -= (q >= kRing) ? kRing : 0;
+                    h += HS(RD + q);
+                    if (i >= 9) nh[i - 9] = h;
+                }
+                const int z = y / L;
+                const float b0 = HS(B0), b1 = HS(B1);
+#pragma unroll 1
+                for (int l = 0; l < 8; l++) {
+                    const int lag = (kP + 1) + (k - 1) * 8 + l;
+                    c2_block_stat(c, lag, HS(ACC + l), b0, b1 - HS(HEAD + l) + nh[l], L, z);
+                    HS(ACC + l) = 0.f;
+                    HS(HEAD + l) = nh[l];
+                }
+                HS(B0) = 0.f;
+                HS(B1) = 0.f;
+            }
+        }
+        if (k + 1 >= kstop) break;
+        if (n & 1) {
+            v0 += HS(PEND0);
+            if (CCF) v1 += HS(PEND1);
+            k++;
+            continue;
+        }
+        HS(PEND0) = v0;
+        if (CCF) HS(PEND1) = v1;
+        break;
+#undef HS
+    }
+}
+
+template <bool CCF>
+__global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
+{
+    extern __shared__ float c2sm[];
+    constexpr int F = CCF ? kTailFieldsCcf : kTailFieldsAcf;
+    constexpr int NCNT = kRing + 8 + 2 + 8 + 1, ACC = kRing;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
+    if (pix >= a.npix) return;          // no block-wide synchronisation below
+    float *hs = c2sm + tid;
+    if (!CCF) inA = inB;
+    C2Ctx c;
+    c2_ctx(c, a, pix, seg, k0);
+    const int s0 = seg << a.seg_log[k0];
+    if (s0 >= a.num) return;
+    const int s1 = min(s0 + (1 << a.seg_log[k0]), a.num);
+    for (int lag = (kP + 1) + (k0 - 1) * 8; lag < a.chanum; lag++)
+        for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
+    for (int k = k0; k < a.q; k++)
+        for (int f = 0; f < F; f++) hs[((size_t)(k - k0) * F + f) * nt] = (f == NCNT) ? (float)(s0 >> k) : 0.f;
+    // the segment's level-k0 samples and the ones the top level's last
+    // direct samples need (16 top-level samples past the segment)
+    const int nk0 = a.numbin[k0];
+    const int beg = s0 >> k0;
+    const int end = min(nk0, (s1 >> k0) + (17 << (a.q - 1 - k0)));
+    for (int n = beg; n < end; n++) {
+        const float vb = __ldg(&inB[(size_t)n * a.npix + pix]);
+        const float va = CCF ? __ldg(&inA[(size_t)n * a.npix + pix]) : vb;
+        c2_tail_push<CCF>(c, a, hs, nt, k0, k0, a.q, s0, s1, va, vb);
+    }
+    // zero samples past the last one until each level's last direct sample of
+    // the segment has been processed (no cascade)
+    for (int k = k0; k < a.q; k++) {
+        const float *s = hs + (size_t)(k - k0) * F * nt;
+        const int want = ((s1 >= a.num) ? a.numbin[k] : (s1 >> k)) + 16;
+        while ((int)s[NCNT * nt] < want) c2_tail_push<CCF>(c, a, hs, nt, k0, k, k + 1, s0, s1, 0.f, 0.f);
+    }
+    for (int k = k0; k < a.q; k++)
+        for (int l = 0; l < 8; l++)
+            c2_add_total(c, (kP + 1) + (k - 1) * 8 + l, hs[((size_t)(k - k0) * F + ACC + l) * nt]);
+}
+
+// ---------------------------------------------------------------------------
+// Finalise: segments combined per (pixel, lag): product totals, block
+// statistics brought to one shift (FP64), outputs as calculateCF
+// (java:9491-9531).
+// ---------------------------------------------------------------------------
+__global__ void c2_finalize_kernel(C2Args a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.npix * a.chanum) return;
+    const int pix = i / a.chanum, lag = i % a.chanum;
+    const int ind = a.blk_ind[pix];
+    const int pnum = a.li->pnum_by_ind[ind];
+    const int level = lag <= kP ? 0 : 1 + (lag - (kP + 1)) / 8;
+    const int sl = a.seg_log[level];
+    const int nseg = (a.num + (1 << sl) - 1) >> sl;
+    double A = 0.0, S1 = 0.0, S2 = 0.0, r = 0.0;
+    bool have_r = false;
+    for (int sg = 0; sg < nseg; sg++) {
+        float *st = a.o.stats + sg * a.stat_stride;
+        A += (double)stat_ref(st, a.npix, lag, 0, pix) + (double)stat_ref(st, a.npix, lag, 1, pix);
+        const int s0 = sg << sl, s1 = min(s0 + (1 << sl), a.num);
+        const int z0 = s0 >> ind, z1 = (s1 + (1 << ind) - 1) >> ind;
+        const int cnt = max(0, min(pnum, z1) - z0);
+        if (cnt == 0) continue;
+        const double rs = stat_ref(st, a.npix, lag, 4, pix);
+        const double s1s = stat_ref(st, a.npix, lag, 2, pix), s2s = stat_ref(st, a.npix, lag, 3, pix);
+        if (!have_r) { r = rs; have_r = true; }
+        const double dr = rs - r;
+        S1 += s1s + cnt * dr;
+        S2 += s2s + 2.0 * dr * s1s + cnt * dr * dr;
+    }
+    const float4 m = a.mon[(size_t)pix * a.chanum + lag];
+    const double n = a.li->prodnum[lag];
+    const double dmDm = (double)m.z * (double)m.w;
+    const double sumprod = A - n * (double)m.x * (double)m.y;
+    const double corav = sumprod / (n * dmDm);
+    const double pn = pnum;
+    const double bv = (S2 / pn - (S1 / pn) * (S1 / pn)) / ((pn - 1) * dmDm * dmDm);
+    double acf = corav;
+    if (a.o.gls) acf = (lag == 0) ? 0.0 : (S1 + pn * r) / (pn * dmDm);   // mcov (java:9526-9531)
+    if (a.o.acf) a.o.acf[(size_t)pix * a.chanum + lag] = acf;
+    if (a.o.var) a.o.var[(size_t)pix * a.chanum + lag] = bv;
+    if (a.o.sd) a.o.sd[(size_t)pix * a.chanum + lag] = sqrt(bv);
+    if (lag == 1) {
+        if (a.o.nb_mean) a.o.nb_mean[pix] = m.z;
+        if (a.o.nb_cov) a.o.nb_cov[pix] = sumprod / n;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+// The chain needs blocks of at least 16 level-0 and 8 level-1 samples
+// (ind >= Q-1 >= 4).
+bool corr2_supported(const Job &j) { return j.p == kP && j.q >= 5; }
+
+namespace {
+struct Plan2 {
+    int npair;                // pair kernels (levels 0-1, then 2-3 when Q >= 7)
+    int k_tail;               // first level of the tail kernel (Q: none)
+    int seg_log[kMaxLevels];
+    int nseg_max;
+};
+
+Plan2 plan2(const Job &j)
+{
+    Plan2 p;
+    const int base = max(j.blocknum - 1, j.q - 1);   // every pixel's block length divides 2^base frames
+    p.npair = (j.q >= 7) ? 2 : 1;
+    p.k_tail = 2 * p.npair;
+    for (int k = 0; k < kMaxLevels; k++) p.seg_log[k] = 0;
+    for (int i = 0; i < p.npair; i++) {
+        const int k = 2 * i;
+        const int sl = max(base, k + 6);            // segments start at multiples of 64 level-k samples
+        p.seg_log[k] = p.seg_log[k + 1] = sl;
+    }
+    if (p.k_tail < j.q) {
+        const int sl = max(base + 2, p.k_tail + 6);  // longer segments: the tail's halo is 17 top-level samples
+        for (int k = p.k_tail; k < j.q; k++) p.seg_log[k] = sl;
+    }
+    p.nseg_max = 1;
+    for (int k = 0; k < j.q; k++)
+        p.nseg_max = max(p.nseg_max, (j.num + (1 << p.seg_log[k]) - 1) >> p.seg_log[k]);
+    return p;
+}
+}  // namespace
+
+int corr2_nseg(const Job &j) { return plan2(j).nseg_max; }
+
+int corr_kernel_count(const Job &j)
+{
+    if (!corr2_supported(j)) return 1;
+    const Plan2 p = plan2(j);
+    return 1 + p.npair + (p.k_tail < j.q ? 1 : 0) + 1;
+}
+
+size_t corr_stats_floats(const Job &j)
+{
+    const size_t one = (size_t)j.chanum * kStatN * j.npix;
+    return corr2_supported(j) ? one * corr2_nseg(j) : one;
+}
+
+// Sample streams: s0 (num x npix), s2 (num/4 x npix), s4 (num/16 x npix), per trace.
+size_t corr_stream_floats(const Job &j)
+{
+    if (!corr2_supported(j)) return 1;
+    const size_t tr = j.is_ccf ? 2 : 1;
+    return tr * (size_t)j.npix * ((size_t)j.num + (size_t)(j.num >> 2) + (size_t)(j.num >> 4) + 3);
+}
+
+cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
+                         const float *basis, const float4 *mon, const int *blk_ind, const CorrOut &o,
+                         float *streams, cudaStream_t stream)
+{
+    const Plan2 pl = plan2(j);
+    C2Args a;
+    memset(&a, 0, sizeof(a));
+    a.o = o;
+    a.mon = mon;
+    a.blk_ind = blk_ind;
+    a.li = li;
+    a.npix = j.npix;
+    a.chanum = j.chanum;
+    a.q = j.q;
+    a.num = j.num;
+    {
+        int nb = j.num;
+        for (int k = 0; k < j.q; k++) { a.numbin[k] = nb; nb /= 2; }
+    }
+    for (int k = 0; k < kMaxLevels; k++) a.seg_log[k] = pl.seg_log[k];
+    a.stat_stride = (size_t)j.chanum * kStatN * j.npix;
+
+    const size_t tr = j.is_ccf ? 2 : 1;
+    const size_t np = j.npix;
+    float *s0a = streams, *s0b = j.is_ccf ? s0a + np * j.num : s0a;
+    float *s2a = streams + tr * np * j.num, *s2b = j.is_ccf ? s2a + np * (j.num >> 2) : s2a;
+    float *s4a = s2a + tr * np * (j.num >> 2), *s4b = j.is_ccf ? s4a + np * (j.num >> 4) : s4a;
+
+    dim3 vgrid((j.npix + 127) / 128, (j.num + kVFrames - 1) / kVFrames);
+    c2_values_kernel<<<vgrid, 128, 0, stream>>>(j, stack, bparams, basis, s0a, s0b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+
+    const int pgx = (j.npix + kC2Threads - 1) / kC2Threads;
+    for (int i = 0; i < pl.npair; i++) {
+        const int k = 2 * i;
+        const float *ia = i ? s2a : s0a, *ib = i ? s2b : s0b;
+        float *oa = (k + 2 < j.q) ? (i ? s4a : s2a) : nullptr;
+        float *ob = (k + 2 < j.q) ? (i ? s4b : s2b) : nullptr;
+        const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k]) - 1) >> pl.seg_log[k]);
+        const bool two = k + 1 < j.q;
+        if (j.is_ccf) {
+            if (i == 0) c2_pair_kernel<true, true, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+            else if (two) c2_pair_kernel<true, false, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+            else c2_pair_kernel<true, false, false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+        } else {
+            if (i == 0) c2_pair_kernel<false, true, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+            else if (two) c2_pair_kernel<false, false, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+            else c2_pair_kernel<false, false, false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (pl.k_tail < j.q) {
+        const int k0 = pl.k_tail;
+        const float *ia = (k0 == 2) ? s2a : s4a, *ib = (k0 == 2) ? s2b : s4b;
+        const int F = j.is_ccf ? kTailFieldsCcf : kTailFieldsAcf;
+        const size_t smem = (size_t)(j.q - k0) * F * kC2Threads * sizeof(float);
+        const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k0]) - 1) >> pl.seg_log[k0]);
+        if (j.is_ccf) {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(c2_tail_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            c2_tail_kernel<true><<<grid, kC2Threads, smem, stream>>>(a, ia, ib, k0);
+        } else {
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(c2_tail_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            c2_tail_kernel<false><<<grid, kC2Threads, smem, stream>>>(a, ia, ib, k0);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    const int n = j.npix * j.chanum;
+    c2_finalize_kernel<<<(n + 255) / 256, 256, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace imfcs

@@ -12,8 +12,12 @@ namespace imfcs {
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
                         const float *basis, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
-                        int pnum_stride, float *stats, int gls, int *err, cudaStream_t stream);
+                        int pnum_stride, float *stats, float *streams, int gls, int *err,
+                        cudaStream_t stream);
 size_t corr_smem_bytes(int q, bool ccf);
+size_t corr_stats_floats(const Job &j);    // per-lag block statistics scratch (floats)
+size_t corr_stream_floats(const Job &j);   // sample streams of the correlator chain (floats)
+int corr_kernel_count(const Job &j);        // kernels one correlator launch issues
 
 struct FitArgs;
 cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream);
