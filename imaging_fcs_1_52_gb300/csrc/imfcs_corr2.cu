@@ -13,8 +13,9 @@
 //             whose positions are compile-time constants inside a 64-sample
 //             unrolled step; it writes the level-(k+2) samples (pair sums of
 //             its level-(k+1) samples) for the next kernel;
-//   tail      levels k0..Q-1 whose blocks may be shorter than 16 samples, one
-//             sample at a time with rings in shared memory;
+//   tail      levels k0..Q-1 (blocks possibly one sample long): one level per
+//             thread, samples built from the level-k0 stream, block
+//             statistics in registers;
 //   finalise  per (pixel, lag): segments combined in FP64, outputs.
 //
 // Products are grouped by their direct sample y (processed when the delayed
@@ -34,9 +35,6 @@ namespace imfcs {
 
 constexpr int kC2Threads = 64;
 constexpr int kVFrames = 256;                // frames per thread in the values pass
-constexpr int kRing = 17;                    // tail rings: samples n-16..n
-constexpr int kTailFieldsAcf = kRing + 8 + 2 + 8 + 2;      // ring, acc, b0, b1, head, pend0, n
-constexpr int kTailFieldsCcf = kTailFieldsAcf + kRing + 1;  // + delayed ring, pend1
 constexpr int kHeadFields = (kP + 1) + 8;                   // first-level heads d = 0..16, second-level d = 9..16
 
 // Arguments shared by the pair, tail and finalise kernels.
@@ -370,130 +368,155 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
 }
 
 // ---------------------------------------------------------------------------
-// Tail kernel: levels k0..Q-1 of one (pixel, segment), one sample at a time.
-// State of level k at hs[((k - k0) * F + f) * nt].
+// Tail kernel: one level k >= k0 of one (pixel, segment) per thread, for the
+// top levels whose blocks may be as short as one sample.  The thread builds
+// its level-k samples from the level-k0 stream (sums of 2^(k-k0) samples),
+// keeps a ring of its last 32 samples in shared memory and its lags' block
+// sums and block statistics in registers; the statistics are written once.
 // ---------------------------------------------------------------------------
 template <bool CCF>
-__device__ __forceinline__ void c2_tail_push(const C2Ctx &c, const C2Args &a, float *hs, int nt, int k0, int k,
-                                             int kstop, int s0, int s1, float v0, float v1)
+__global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
 {
-    constexpr int F = CCF ? kTailFieldsCcf : kTailFieldsAcf;
-    constexpr int RING0 = 0, ACC = kRing, B0 = ACC + 8, B1 = B0 + 1, HEAD = B1 + 1, PEND0 = HEAD + 8,
-                  NCNT = PEND0 + 1, RING1 = NCNT + 1, PEND1 = RING1 + kRing;
-    for (;;) {
-        float *s = hs + (size_t)(k - k0) * F * nt;
-#define HS(f) s[(f) * nt]
-        const int n = (int)HS(NCNT);
-        HS(NCNT) = (float)(n + 1);
-        if (n >= a.numbin[k]) { v0 = 0.f; v1 = 0.f; }
-        const int pos = n % kRing;
-        HS(RING0 + pos) = v0;
-        if (CCF) HS(RING1 + pos) = v1;
-        const int RD = CCF ? RING1 : RING0;      // delayed-trace ring
-        const int y = n - 16;
-        const int ys0 = s0 >> k, ys1 = (s1 >= a.num) ? a.numbin[k] : (s1 >> k);   // segment's direct samples
-        if (y >= ys0 && y < ys1) {
-            const int base = (pos + 1 == kRing) ? 0 : pos + 1;   // ring position of sample y
-            if (y == ys0) {
-                float h = 0.f;
-                for (int i = 0; i < 16; i++) {
-                    int q = base + i;
-                    q -= (q >= kRing) ? kRing : 0;
-                    h += HS(RD + q);
-                    if (i + 1 >= 9) HS(HEAD + i + 1 - 9) = h;
+    __shared__ float ring_sm[(CCF ? 2 : 1) * 32 * kC2Threads];
+    const int tid = threadIdx.x;
+    const int pix = blockIdx.x * kC2Threads + tid, seg = blockIdx.y, k = k0 + blockIdx.z;
+    if (pix >= a.npix || k >= a.q) return;          // no block-wide synchronisation below
+    float *rb = ring_sm + tid;
+    float *ra = CCF ? ring_sm + 32 * kC2Threads + tid : rb;
+    if (!CCF) inA = inB;
+    C2Ctx c;
+    c2_ctx(c, a, pix, seg, k);
+    const int s0 = seg << a.seg_log[k];
+    if (s0 >= a.num) return;
+    const int s1 = min(s0 + (1 << a.seg_log[k]), a.num);
+    const int nkk = a.numbin[k], nk0 = a.numbin[k0];
+    const int ys0 = s0 >> k, ys1 = (s1 >= a.num) ? nkk : (s1 >> k);
+    const int m = 1 << (k - k0);
+    const int lag0 = (kP + 1) + (k - 1) * 8;
+    const int lk = c.ind - k;
+    const int L = lk > 0 ? (1 << lk) : 1;
+
+    float ma[8], mb[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) {
+        const float4 mm = __ldg(&c.mon[lag0 + l]);
+        ma[l] = mm.x;
+        mb[l] = mm.y;
+    }
+    float acc[8], head[8], thi[8], tlo[8], S1[8], S2[8], rr[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) {
+        acc[l] = head[l] = thi[l] = tlo[l] = S1[l] = S2[l] = rr[l] = 0.f;
+    }
+    float b0 = 0.f, b1 = 0.f;
+
+    // samples ys0 .. ys1 + 15 (the last direct samples' delayed partners);
+    // samples from nkk on are zero.  Loads are issued 8 samples at a time.
+    const int nend = ys1 + 16;
+#pragma unroll 1
+    for (int nb = ys0; nb < nend; nb += 8) {
+        float vb[8], va[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            vb[u] = 0.f;
+            va[u] = 0.f;
+            const int n = nb + u;
+            if (n < nkk && n < nend) {
+                if (m <= 8) {
+                    // pairwise sums, as the levels are built (java:9467-9476)
+                    float wb[8], wa[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int q = n * m + i;
+                        const bool in = i < m && q < nk0;
+                        wb[i] = in ? __ldg(&inB[(size_t)q * a.npix + pix]) : 0.f;
+                        wa[i] = (CCF && in) ? __ldg(&inA[(size_t)q * a.npix + pix]) : 0.f;
+                    }
+#pragma unroll
+                    for (int w = 1; w < 8; w *= 2)
+#pragma unroll
+                        for (int i = 0; i < 8; i += 2 * w) {
+                            wb[i] += wb[i + w];
+                            wa[i] += wa[i + w];
+                        }
+                    vb[u] = wb[0];
+                    va[u] = wa[0];
+                } else {
+                    for (int i = 0; i < m; i++) {
+                        const int q = n * m + i;
+                        if (q < nk0) {
+                            vb[u] += __ldg(&inB[(size_t)q * a.npix + pix]);
+                            if (CCF) va[u] += __ldg(&inA[(size_t)q * a.npix + pix]);
+                        }
+                    }
                 }
             }
-            const float x0 = HS(RING0 + base);
-            float x1[8];
+        }
 #pragma unroll
-            for (int l = 0; l < 8; l++) {
-                int q = base + 9 + l;
-                q -= (q >= kRing) ? kRing : 0;
-                x1[l] = HS(RD + q);
+        for (int u = 0; u < 8; u++) {
+            const int n = nb + u;
+            if (n >= nend) break;
+            rb[(n & 31) * kC2Threads] = vb[u];
+            if (CCF) ra[(n & 31) * kC2Threads] = va[u];
+            const int y = n - 16;
+            if (y < ys0) continue;
+            if (y == ys0) {
+                float h = 0.f;
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    h += rb[((y + i) & 31) * kC2Threads];
+                    if (i + 1 >= 9) head[i + 1 - 9] = h;
+                }
             }
+            const float x0 = ra[(y & 31) * kC2Threads];
 #pragma unroll
-            for (int l = 0; l < 8; l++) HS(ACC + l) = fmaf(x0, x1[l], HS(ACC + l));
-            HS(B0) += x0;
-            HS(B1) += HS(RD + base);
-            const int lk = c.ind - k;
-            const int L = lk > 0 ? (1 << lk) : 1;
+            for (int l = 0; l < 8; l++) acc[l] = fmaf(x0, rb[((y + 9 + l) & 31) * kC2Threads], acc[l]);
+            b0 += x0;
+            b1 += rb[(y & 31) * kC2Threads];
             if (((y + 1) & (L - 1)) == 0) {
                 // heads of the next block: sums of the delayed samples y+1 .. y+d
                 float nh[8], h = 0.f;
 #pragma unroll
                 for (int i = 1; i <= 16; i++) {
-                    int q = base + i;
-                    q -= (q >= kRing) ? kRing : 0;
-                    h += HS(RD + q);
+                    h += rb[((y + i) & 31) * kC2Threads];
                     if (i >= 9) nh[i - 9] = h;
                 }
                 const int z = y / L;
-                const float b0 = HS(B0), b1 = HS(B1);
-#pragma unroll 1
+                const bool stat = z < c.pnum;
+#pragma unroll
                 for (int l = 0; l < 8; l++) {
-                    const int lag = (kP + 1) + (k - 1) * 8 + l;
-                    c2_block_stat(c, lag, HS(ACC + l), b0, b1 - HS(HEAD + l) + nh[l], L, z);
-                    HS(ACC + l) = 0.f;
-                    HS(HEAD + l) = nh[l];
+                    const float D = b1 - head[l] + nh[l];
+                    const float P = (acc[l] - mb[l] * b0 - ma[l] * D + (float)L * ma[l] * mb[l]) / (float)L;
+                    ff t = {thi[l], tlo[l]};
+                    ff_add(t, acc[l]);
+                    thi[l] = t.hi;
+                    tlo[l] = t.lo;
+                    if (stat) {
+                        if (z == c.zfirst) rr[l] = P;
+                        const float dv = P - rr[l];
+                        S1[l] += dv;
+                        S2[l] = fmaf(dv, dv, S2[l]);
+                        if (c.gls)
+                            c.bprod[((size_t)pix * (c.chanum - 1) + (lag0 + l - 1)) * c.pnum_stride + z] = P;
+                    }
+                    head[l] = nh[l];
+                    acc[l] = 0.f;
                 }
-                HS(B0) = 0.f;
-                HS(B1) = 0.f;
+                b0 = 0.f;
+                b1 = 0.f;
             }
         }
-        if (k + 1 >= kstop) break;
-        if (n & 1) {
-            v0 += HS(PEND0);
-            if (CCF) v1 += HS(PEND1);
-            k++;
-            continue;
-        }
-        HS(PEND0) = v0;
-        if (CCF) HS(PEND1) = v1;
-        break;
-#undef HS
     }
-}
-
-template <bool CCF>
-__global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
-{
-    extern __shared__ float c2sm[];
-    constexpr int F = CCF ? kTailFieldsCcf : kTailFieldsAcf;
-    constexpr int NCNT = kRing + 8 + 2 + 8 + 1, ACC = kRing;
-    const int nt = blockDim.x, tid = threadIdx.x;
-    const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
-    if (pix >= a.npix) return;          // no block-wide synchronisation below
-    float *hs = c2sm + tid;
-    if (!CCF) inA = inB;
-    C2Ctx c;
-    c2_ctx(c, a, pix, seg, k0);
-    const int s0 = seg << a.seg_log[k0];
-    if (s0 >= a.num) return;
-    const int s1 = min(s0 + (1 << a.seg_log[k0]), a.num);
-    for (int lag = (kP + 1) + (k0 - 1) * 8; lag < a.chanum; lag++)
-        for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
-    for (int k = k0; k < a.q; k++)
-        for (int f = 0; f < F; f++) hs[((size_t)(k - k0) * F + f) * nt] = (f == NCNT) ? (float)(s0 >> k) : 0.f;
-    // the segment's level-k0 samples and the ones the top level's last
-    // direct samples need (16 top-level samples past the segment)
-    const int nk0 = a.numbin[k0];
-    const int beg = s0 >> k0;
-    const int end = min(nk0, (s1 >> k0) + (17 << (a.q - 1 - k0)));
-    for (int n = beg; n < end; n++) {
-        const float vb = __ldg(&inB[(size_t)n * a.npix + pix]);
-        const float va = CCF ? __ldg(&inA[(size_t)n * a.npix + pix]) : vb;
-        c2_tail_push<CCF>(c, a, hs, nt, k0, k0, a.q, s0, s1, va, vb);
+#pragma unroll
+    for (int l = 0; l < 8; l++) {
+        ff t = {thi[l], tlo[l]};
+        ff_add(t, acc[l]);
+        stat_ref(c.stats, c.npix, lag0 + l, 0, pix) = t.hi;
+        stat_ref(c.stats, c.npix, lag0 + l, 1, pix) = t.lo;
+        stat_ref(c.stats, c.npix, lag0 + l, 2, pix) = S1[l];
+        stat_ref(c.stats, c.npix, lag0 + l, 3, pix) = S2[l];
+        stat_ref(c.stats, c.npix, lag0 + l, 4, pix) = rr[l];
     }
-    // zero samples past the last one until each level's last direct sample of
-    // the segment has been processed (no cascade)
-    for (int k = k0; k < a.q; k++) {
-        const float *s = hs + (size_t)(k - k0) * F * nt;
-        const int want = ((s1 >= a.num) ? a.numbin[k] : (s1 >> k)) + 16;
-        while ((int)s[NCNT * nt] < want) c2_tail_push<CCF>(c, a, hs, nt, k0, k, k + 1, s0, s1, 0.f, 0.f);
-    }
-    for (int k = k0; k < a.q; k++)
-        for (int l = 0; l < 8; l++)
-            c2_add_total(c, (kP + 1) + (k - 1) * 8 + l, hs[((size_t)(k - k0) * F + ACC + l) * nt]);
 }
 
 // ---------------------------------------------------------------------------
@@ -573,7 +596,7 @@ Plan2 plan2(const Job &j)
         p.seg_log[k] = p.seg_log[k + 1] = sl;
     }
     if (p.k_tail < j.q) {
-        const int sl = max(base + 2, p.k_tail + 6);  // longer segments: the tail's halo is 17 top-level samples
+        const int sl = max(base, p.k_tail);
         for (int k = p.k_tail; k < j.q; k++) p.seg_log[k] = sl;
     }
     p.nseg_max = 1;
@@ -662,18 +685,9 @@ cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, con
     if (pl.k_tail < j.q) {
         const int k0 = pl.k_tail;
         const float *ia = (k0 == 2) ? s2a : s4a, *ib = (k0 == 2) ? s2b : s4b;
-        const int F = j.is_ccf ? kTailFieldsCcf : kTailFieldsAcf;
-        const size_t smem = (size_t)(j.q - k0) * F * kC2Threads * sizeof(float);
-        const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k0]) - 1) >> pl.seg_log[k0]);
-        if (j.is_ccf) {
-            if (smem > 48 * 1024)
-                cudaFuncSetAttribute(c2_tail_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            c2_tail_kernel<true><<<grid, kC2Threads, smem, stream>>>(a, ia, ib, k0);
-        } else {
-            if (smem > 48 * 1024)
-                cudaFuncSetAttribute(c2_tail_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            c2_tail_kernel<false><<<grid, kC2Threads, smem, stream>>>(a, ia, ib, k0);
-        }
+        const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k0]) - 1) >> pl.seg_log[k0], j.q - k0);
+        if (j.is_ccf) c2_tail_kernel<true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
+        else c2_tail_kernel<false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -355,7 +355,8 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                 const bool finite = isfinite(sn.chi2);
                 const bool better = finite && sn.chi2 < s.chi2;
                 if (gpufit) {
-                    // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487)
+                    // Gpufit semantics (agpufitjni.cu:2289-2320, 2458-2487);
+                    // the ACF model then gets the FP64-residual finish below
                     bool found = finite && fabs(sn.chi2 - s.chi2) < (double)a.tol * fmax(1.0, sn.chi2);
                     if (better) {
                         for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
@@ -364,11 +365,20 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                     } else {
                         lambda *= 10.f;
                     }
-                    if (found) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                    if (lambda > 1e30f) { state = IMFCS_STATE_CONVERGED; it++; break; }
-                    continue;
+                    if (found || lambda > 1e30f) {
+                        if (a.model == IMFCS_MODEL_ACF_1D && !precise) {
+                            to_precise = true;
+                        } else {
+                            state = IMFCS_STATE_CONVERGED;
+                            it++;
+                            break;
+                        }
+                    }
+                    if (!to_precise) continue;
                 }
-                if (better) {
+                if (gpufit) {
+                    // handled above
+                } else if (better) {
                     for (int i = 0; i < a.np; i++) { pard[i] = pnd[i]; par[i] = pnf[i]; }
                     s = sn;
                     lambda = fmaxf(lambda * 0.1f, 1e-9f);
@@ -382,6 +392,68 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                 if (nprec > 60) { state = IMFCS_STATE_CONVERGED; it++; break; }
             }
             if (to_precise) {
+                // Newton steps on the FP64-residual gradient with the Hessian
+                // of chi^2/2, H = -dg/dp, from forward differences (0.1 sigma)
+                // of the FP32 gradient: converges in a few steps where
+                // Gauss-Newton contracts only linearly on a non-zero residual.
+                float H[KM * KM];
+#pragma unroll
+                for (int i = 0; i < KM * KM; i++) H[i] = 0.f;
+                for (int i = 0; i < a.k; i++) {
+                    float sgi = 0.f;
+#pragma unroll
+                    for (int q = 0; q < KM; q++)
+                        if (q == i) sgi = rsqrtf(fmaxf(s.A[q * KM + q], 1e-30f));
+                    const float eps = 0.1f * sgi;
+                    float pe[IMFCS_NPARAM];
+                    double pde[IMFCS_NPARAM];
+                    for (int q = 0; q < a.np; q++) { pe[q] = par[q]; pde[q] = pard[q]; }
+                    pde[a.idx[i]] += (double)eps;
+                    pe[a.idx[i]] = (float)pde[a.idx[i]];
+                    const float de = (float)(pde[a.idx[i]] - pard[a.idx[i]]);
+                    LMState<KM> se;
+                    evaluate<KM>(a, mc, mcd, pe, pde, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, se, c2, c3, false,
+                                 yg, wg);
+#pragma unroll
+                    for (int r = 0; r < KM; r++)
+#pragma unroll
+                        for (int q = 0; q < KM; q++)
+                            if (q == i) H[r * KM + q] = (s.g[r] - se.g[r]) / de;
+                }
+#pragma unroll
+                for (int r = 0; r < KM; r++)
+#pragma unroll
+                    for (int q = 0; q < r; q++) {
+                        const float v = 0.5f * (H[r * KM + q] + H[q * KM + r]);
+                        H[r * KM + q] = v;
+                        H[q * KM + r] = v;
+                    }
+                bool newton_done = false;
+#pragma unroll 1
+                for (int ni = 0; ni < 4; ni++) {
+                    evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true,
+                                 yg, wg);
+                    float hn[KM];
+                    if (!isfinite(s.chi2) || !solve_scaled<KM>(H, s.g, a.k, 0.f, hn)) break;
+                    bool conv = true;
+#pragma unroll
+                    for (int i = 0; i < KM; i++)
+                        if (i < a.k) {
+                            const float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
+                            conv = conv && (fabsf(hn[i]) <= 1e-7f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
+                            if (!(fabsf(hn[i]) <= 0.05f * sig)) ni = 4;   // not in the quadratic region
+                        }
+                    if (ni >= 4) break;
+#pragma unroll
+                    for (int i = 0; i < KM; i++)
+                        if (i < a.k) {
+                            pard[a.idx[i]] += (double)hn[i];
+                            par[a.idx[i]] = (float)pard[a.idx[i]];
+                        }
+                    if (conv) { newton_done = true; break; }
+                }
+                if (newton_done) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                // otherwise: Levenberg-Marquardt on the FP64-residual model
                 precise = true;
                 evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true,
                              yg, wg);

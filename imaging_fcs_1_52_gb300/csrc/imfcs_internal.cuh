@@ -251,6 +251,14 @@ __device__ __forceinline__ void lateral_1d_f(float a, float r, float v, float ta
                                              float inv_p0, float &L, float &dL_dp0, float &dL_dv)
 {
     const float inv_sqrtpi = 0.5641895835477563f;
+    if (r == 0.f && v == 0.f) {   // autocorrelation without flow: the three terms collapse to two
+        const float u = a * inv_p0;
+        const float m = expm1f(-u * u), er = erff(u);
+        L = 2.f * (p0 * inv_sqrtpi * m + a * er);
+        dL_dp0 = 2.f * m * inv_sqrtpi;
+        dL_dv = 0.f;   // (er2 + 2 er3 - er1) tau with er1 = er2, er3 = 0
+        return;
+    }
     float p1 = a + r - v * tau, p2 = a - r + v * tau, p3 = r - v * tau;
     float u1 = p1 * inv_p0, u2 = p2 * inv_p0, u3 = p3 * inv_p0;
     float m1 = expm1f(-u1 * u1), m2 = expm1f(-u2 * u2), m3 = expm1f(-u3 * u3);
@@ -272,7 +280,11 @@ __device__ __forceinline__ void component_f(float d, float vx, float vy, const M
     float inv_p0 = 1.f / p0;
     float Lx, Ly, dLx0, dLy0, dLxv, dLyv;
     lateral_1d_f(c.ax, c.rx, vx, tau, p0, inv_p0, Lx, dLx0, dLxv);
-    lateral_1d_f(c.ay, c.ry, vy, tau, p0, inv_p0, Ly, dLy0, dLyv);
+    if (c.ay == c.ax && c.ry == c.rx && vy == vx) {   // square window, same offset and flow: same term
+        Ly = Lx; dLy0 = dLx0; dLyv = dLxv;
+    } else {
+        lateral_1d_f(c.ay, c.ry, vy, tau, p0, inv_p0, Ly, dLy0, dLyv);
+    }
     float dp0 = 2.f * tau * inv_p0;
     float lat = Lx * Ly * c.inv_norm;
     float dlat_dd = (dLx0 * Ly + Lx * dLy0) * dp0 * c.inv_norm;
@@ -330,6 +342,10 @@ struct ModelConstD {
 __device__ __forceinline__ double lateral_1d_d(double a, double r, double v, double tau, double p0)
 {
     const double inv_sqrtpi = 0.56418958354775628695;
+    if (r == 0.0 && v == 0.0) {   // autocorrelation without flow: the three terms collapse to two
+        const double u = a / p0;
+        return 2.0 * (p0 * inv_sqrtpi * expm1(-u * u) + a * erf(u));
+    }
     double p1 = a + r - v * tau, p2 = a - r + v * tau, p3 = r - v * tau;
     double u1 = p1 / p0, u2 = p2 / p0, u3 = p3 / p0;
     double e = expm1(-u1 * u1) + expm1(-u2 * u2) - 2.0 * expm1(-u3 * u3);
@@ -339,7 +355,9 @@ __device__ __forceinline__ double lateral_1d_d(double a, double r, double v, dou
 __device__ __forceinline__ double component_d(double d, double vx, double vy, const ModelConstD &c, double tau)
 {
     double p0 = sqrt(4.0 * d * tau + c.s * c.s);
-    double lat = lateral_1d_d(c.ax, c.rx, vx, tau, p0) * lateral_1d_d(c.ay, c.ry, vy, tau, p0) * c.inv_norm;
+    const double lx = lateral_1d_d(c.ax, c.rx, vx, tau, p0);
+    const double ly = (c.ay == c.ax && c.ry == c.rx && vy == vx) ? lx : lateral_1d_d(c.ay, c.ry, vy, tau, p0);
+    double lat = lx * ly * c.inv_norm;
     return lat / sqrt(1.0 + 4.0 * d * tau / (c.sz * c.sz));
 }
 

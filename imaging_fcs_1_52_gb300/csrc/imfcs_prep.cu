@@ -129,15 +129,15 @@ __global__ void center_kernel(Job j, const float *trace, float *bp_out)
 // Scaled variables t / tmax, y / ymax; one warp per trace.
 //   phase 1: FP32 model and normal equations until the Gauss-Newton step is
 //            below 1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
-//   phase 2: model values and residuals in FP64 (the exponentials by a
-//            per-lane recurrence), Jacobian and normal equations in FP32,
+//   phase 2: model values and residuals in float-float (the exponentials by
+//            a per-lane recurrence), Jacobian and normal equations in FP32,
 //            until the step is below 1e-5 sigma + 1e-7 |p|.
 // A rate at its bound k = 0 whose Gauss-Newton step points below it is held
 // fixed (active set).
 // ---------------------------------------------------------------------------
 
-// u = (1 - e^{-kt}) / k and du/dk in FP32, x = k t >= 0.
-__device__ __forceinline__ void exp_u_f(float k, float t, float &u, float &dudk)
+// u = (1 - e^{-kt}) / k and du/dk in FP32, x = k t >= 0 (ik = 1/k).
+__device__ __forceinline__ void exp_u_f(float k, float ik, float t, float &u, float &dudk)
 {
     const float x = k * t;
     if (x < 0.05f) {
@@ -149,14 +149,14 @@ __device__ __forceinline__ void exp_u_f(float k, float t, float &u, float &dudk)
         d = fmaf(x, d, 0.5f);
         dudk = -t * t * d;
     } else {
-        const float em = expm1f(-x);
-        u = -em / k;
-        dudk = (t * (1.f + em) - u) / k;
+        const float em = (x < 0.7f) ? expm1f(-x) : __expf(-x) - 1.f;
+        u = -em * ik;
+        dudk = (t * (1.f + em) - u) * ik;
     }
 }
 
 // du/dk from an FP32 copy of e = e^{-kt} and u (series for small x).
-__device__ __forceinline__ float exp_dudk(float k, float t, float e, float u)
+__device__ __forceinline__ float exp_dudk(float k, float ik, float t, float e, float u)
 {
     const float x = k * t;
     if (x < 0.05f) {
@@ -166,7 +166,45 @@ __device__ __forceinline__ float exp_dudk(float k, float t, float e, float u)
         d = fmaf(x, d, 0.5f);
         return -t * t * d;
     }
-    return (t * e - u) / k;
+    return (t * e - u) * ik;
+}
+
+// Float-float (double-single) arithmetic for the precise residuals: exact
+// two-sum / two-product (Knuth, Dekker) with explicitly rounded operations.
+struct f2 {
+    float hi, lo;
+};
+__device__ __forceinline__ f2 f2_quick(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ f2 f2_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ f2 f2_two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
+{
+    f2 s = f2_two_sum(a.hi, b.hi);
+    return f2_quick(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ f2 f2_neg(f2 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 p = f2_two_prod(a.hi, b.hi);
+    return f2_quick(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
+}
+__device__ __forceinline__ f2 f2_from_d(double x)
+{
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
 }
 
 // (A + lambda diag(A) + ridge) x = b on the Jacobi-scaled system, FP32;
@@ -207,7 +245,9 @@ __device__ bool solve_scaled_k(const float *A, const float *b, float lambda, uns
 }
 
 // chi^2 and the normal equations A = J^T J, g = J^T r of the scaled model at
-// p over the trace (warp); precise: FP64 model values and residuals.
+// p over the trace (warp).  precise: model values and residuals in
+// float-float (the exponentials by a per-lane recurrence e <- e q seeded in
+// FP64), chi^2 summed in float-float; otherwise FP32.
 template <int K>
 __device__ double exp_normal(const float *y, int n, float dts, float iy, const double *p, bool precise,
                              float *A, float *g, int lane)
@@ -216,20 +256,24 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
     constexpr int NA = K * (K + 1) / 2 + K;
     float acc[NA];
     for (int i = 0; i < NA; i++) acc[i] = 0.f;
-    float pf[K];
+    float pf[K], ik[NC];
     for (int i = 0; i < K; i++) pf[i] = (float)p[i];
-    double e[NC], q[NC], invk[NC];
+    for (int c = 0; c < NC; c++) ik[c] = 1.f / pf[2 + 2 * c];
+    f2 e[NC], q[NC], invk[NC], sp[NC], f0;
     bool slow[NC];
     if (precise) {
+        f0 = f2_from_d(p[0]);
         for (int c = 0; c < NC; c++) {
             const double k = p[2 + 2 * c];
-            e[c] = exp(-k * ((double)lane + 0.5) * (double)dts);
-            q[c] = exp(-k * 32.0 * (double)dts);
+            e[c] = f2_from_d(exp(-k * ((double)lane + 0.5) * (double)dts));
+            q[c] = f2_from_d(exp(-k * 32.0 * (double)dts));
             slow[c] = k * (double)n * (double)dts < 1e-4;
-            invk[c] = slow[c] ? 0.0 : 1.0 / k;
+            invk[c] = f2_from_d(slow[c] ? 0.0 : 1.0 / k);
+            sp[c] = f2_from_d(p[1 + 2 * c]);
         }
     }
-    double c2 = 0.0;
+    double c2d = 0.0;
+    f2 c2 = {0.f, 0.f};
     for (int x = lane; x < n; x += 32) {
         const float t = ((float)x + 0.5f) * dts;
         float gr[K], r;
@@ -238,34 +282,35 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
             float f = pf[0];
             for (int c = 0; c < NC; c++) {
                 float u, du;
-                exp_u_f(pf[2 + 2 * c], t, u, du);
+                exp_u_f(pf[2 + 2 * c], ik[c], t, u, du);
                 f -= pf[1 + 2 * c] * u;
                 gr[1 + 2 * c] = -u;
                 gr[2 + 2 * c] = -pf[1 + 2 * c] * du;
             }
             r = __ldg(&y[x]) * iy - f;
-            c2 += (double)r * (double)r;
+            c2d += (double)(r * r);
         } else {
-            const double td = ((double)x + 0.5) * (double)dts;
-            double f = p[0];
+            const f2 tf = f2_two_prod((float)x + 0.5f, dts);
+            f2 f = f0;
             for (int c = 0; c < NC; c++) {
-                const double k = p[2 + 2 * c];
-                double u;
+                f2 u;
                 if (slow[c]) {
-                    const double xx = k * td;
-                    u = td * (1.0 - xx * (0.5 - xx * (1.0 / 6.0 - xx * (1.0 / 24.0))));
+                    // u = t (1 - corr), corr = x/2 - x^2/6 + x^3/24 (x < 1e-4)
+                    const float xx = pf[2 + 2 * c] * t;
+                    const float corr = xx * (0.5f - xx * (1.f / 6.f - xx * (1.f / 24.f)));
+                    u = f2_add(tf, f2_neg(f2_two_prod(tf.hi, corr)));
                 } else {
-                    u = (1.0 - e[c]) * invk[c];
+                    u = f2_mul(f2_add({1.f, 0.f}, f2_neg(e[c])), invk[c]);
                 }
-                f -= p[1 + 2 * c] * u;
-                const float uf = (float)u;
+                f = f2_add(f, f2_neg(f2_mul(sp[c], u)));
+                const float uf = u.hi + u.lo;
                 gr[1 + 2 * c] = -uf;
-                gr[2 + 2 * c] = -pf[1 + 2 * c] * exp_dudk(pf[2 + 2 * c], t, (float)e[c], uf);
-                e[c] *= q[c];
+                gr[2 + 2 * c] = -pf[1 + 2 * c] * exp_dudk(pf[2 + 2 * c], ik[c], t, e[c].hi + e[c].lo, uf);
+                e[c] = f2_mul(e[c], q[c]);
             }
-            const double rd = (double)__ldg(&y[x]) * (double)iy - f;
-            r = (float)rd;
-            c2 += rd * rd;
+            const f2 rr = f2_add(f2_two_prod(__ldg(&y[x]), iy), f2_neg(f));
+            r = rr.hi + rr.lo;
+            c2 = f2_add(c2, f2_mul(rr, rr));
         }
         int qa = 0;
         for (int a = 0; a < K; a++)
@@ -280,7 +325,8 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
             A[b * K + a] = v;
         }
     for (int a = 0; a < K; a++) g[a] = warp_sum(acc[qa++]);
-    return warp_sum_d(c2);
+    if (precise) c2d = (double)c2.hi + (double)c2.lo;
+    return warp_sum_d(c2d);
 }
 
 // Held rates (bit mask) and the undamped Gauss-Newton step.
