@@ -130,8 +130,8 @@ def measured_peaks():
 
 
 def load_profile_traffic():
-    """DRAM bytes per correlator launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "corr_kernel_traffic.json")
+    """DRAM bytes per correlator-chain launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "correlator_chain_traffic.json")
     if os.path.exists(p):
         try:
             return float(json.load(open(p))["bytes_per_launch_full_size"])
@@ -265,7 +265,7 @@ def main():
     if rank == 0:
         peak, peak_kind = measured_peaks()
         corr_avg = statistics.mean(corr_ms)
-        # algorithmic bytes of one correlator launch: the uint16 stack once +
+        # algorithmic bytes of one correlator stage: the uint16 stack once +
         # ACF and blocked variance out (8 B each per pixel and channel)
         alg_bytes = T * H * W * 2 + cfg.npix * cfg.chanum * 8 * 2
         achieved = alg_bytes / (corr_avg * 1e-3) / 1e9
@@ -287,7 +287,8 @@ def main():
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": launches,
             "stages_ms": {k: v / args.steps for k, v in stage_acc.items()},
-            "roofline": {"kernel": "corr_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+            "roofline": {"kernel": "correlator chain (c2_values, c2_pair x2, c2_tail, c2_finalize)",
+                         "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": load_profile_traffic(),
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": corr_avg},
