@@ -83,7 +83,8 @@ __device__ __forceinline__ double model_eval(const FitArgs &a, const ModelConst 
 // Jacobian are first transformed by L^-1 held in shared memory (packed lower
 // triangle); y then holds the transformed data.
 template <int KM>
-__device__ __forceinline__ void accumulate_point(float *acc, double &c2acc, const float *gr, double rd, float w)
+__device__ __forceinline__ void accumulate_point(float *acc, double &c2acc, float &c2f, const float *gr, double rd,
+                                                 float w, bool precise)
 {
     float r = (float)rd;
     int q = 0;
@@ -93,7 +94,8 @@ __device__ __forceinline__ void accumulate_point(float *acc, double &c2acc, cons
         for (int t = 0; t <= p; t++) acc[q++] += w * gr[p] * gr[t];
 #pragma unroll
     for (int p = 0; p < KM; p++) acc[q++] += w * gr[p] * r;
-    c2acc += (double)w * rd * rd;
+    if (precise) c2acc += (double)w * rd * rd;
+    else c2f = fmaf(w * r, r, c2f);       // FP32 phase: a few points per lane
 }
 
 // yg/wg (non-null): the fit's data are read from global memory point by point
@@ -107,6 +109,7 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
     constexpr int NACC = KM * (KM + 1) / 2 + KM;
     float acc[NACC];
     double c2acc = 0.0;
+    float c2f = 0.f;
 #pragma unroll
     for (int i = 0; i < NACC; i++) acc[i] = 0.f;
     const int n = a.npts;
@@ -114,7 +117,7 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
         for (int i = lane; i < n; i += 32) {
             float gr[KM];
             double f = model_eval<KM>(a, mc, mcd, par, pard, __ldg(&a.x[i]), gr, c2, c3, precise);
-            accumulate_point<KM>(acc, c2acc, gr, (double)__ldg(&yg[i]) - f, wg ? __ldg(&wg[i]) : 1.f);
+            accumulate_point<KM>(acc, c2acc, c2f, gr, (double)__ldg(&yg[i]) - f, wg ? __ldg(&wg[i]) : 1.f, precise);
         }
     } else if (!sh_linv) {
 #pragma unroll
@@ -123,7 +126,12 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
             if (i < n) {
                 float gr[KM];
                 double f = model_eval<KM>(a, mc, mcd, par, pard, xl[m], gr, c2, c3, precise);
-                accumulate_point<KM>(acc, c2acc, gr, (double)yl[m] - f, wl[m]);
+                if (precise) {
+                    accumulate_point<KM>(acc, c2acc, c2f, gr, (double)yl[m] - f, wl[m], true);
+                } else {
+                    // FP32 phase: FP32 residual, no FP64 operation per point
+                    accumulate_point<KM>(acc, c2acc, c2f, gr, (double)(yl[m] - (float)f), wl[m], false);
+                }
             }
         }
     } else {
@@ -179,7 +187,7 @@ __device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelCons
         }
 #pragma unroll
     for (int p = 0; p < KM; p++) s.g[p] = warp_sum(acc[q++]);
-    s.chi2 = precise ? warp_sum_d(c2acc) : (double)warp_sum((float)c2acc);
+    s.chi2 = precise ? warp_sum_d(c2acc + (double)c2f) : (double)warp_sum(c2f + (float)c2acc);
 }
 
 // (A + lambda diag(A)) h = g, solved in FP32 on the Jacobi-scaled system

@@ -273,6 +273,7 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
         }
     }
     double c2d = 0.0;
+    float c2f = 0.f;            // FP32 phase: per-lane sum of ~n/32 squares
     f2 c2 = {0.f, 0.f};
     for (int x = lane; x < n; x += 32) {
         const float t = ((float)x + 0.5f) * dts;
@@ -288,7 +289,7 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
                 gr[2 + 2 * c] = -pf[1 + 2 * c] * du;
             }
             r = __ldg(&y[x]) * iy - f;
-            c2d += (double)(r * r);
+            c2f = fmaf(r, r, c2f);
         } else {
             const f2 tf = f2_two_prod((float)x + 0.5f, dts);
             f2 f = f0;
@@ -325,7 +326,7 @@ __device__ double exp_normal(const float *y, int n, float dts, float iy, const d
             A[b * K + a] = v;
         }
     for (int a = 0; a < K; a++) g[a] = warp_sum(acc[qa++]);
-    if (precise) c2d = (double)c2.hi + (double)c2.lo;
+    c2d = precise ? (double)c2.hi + (double)c2.lo : (double)c2f;
     return warp_sum_d(c2d);
 }
 
