@@ -101,7 +101,7 @@ __device__ __forceinline__ void accumulate_point(float *acc, double &c2acc, floa
 // yg/wg (non-null): the fit's data are read from global memory point by point
 // (fits with more than kMaxPts points, no GLS transform).
 template <int KM>
-__device__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd, const float *par,
+__device__ __noinline__ void evaluate(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd, const float *par,
                          const double *pard, const float *yl, const float *wl, const float *xl, int lane,
                          float *sh_fj, double *sh_f64, const float *sh_linv, LMState<KM> &s, bool c2,
                          bool c3, bool precise, const float *yg = nullptr, const float *wg = nullptr)

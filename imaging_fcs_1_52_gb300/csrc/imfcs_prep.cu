@@ -249,7 +249,7 @@ __device__ bool solve_scaled_k(const float *A, const float *b, float lambda, uns
 // float-float (the exponentials by a per-lane recurrence e <- e q seeded in
 // FP64), chi^2 summed in float-float; otherwise FP32.
 template <int K>
-__device__ double exp_normal(const float *y, int n, float dts, float iy, const double *p, bool precise,
+__device__ __noinline__ double exp_normal(const float *y, int n, float dts, float iy, const double *p, bool precise,
                              float *A, float *g, int lane)
 {
     constexpr int NC = (K - 1) / 2;
