@@ -1,12 +1,13 @@
 """Benchmark: ACF + fit pixels/s on a 128 x 128 x 50,000-frame uint16 stack.
 
 Workload (the plain method at scale): a seeded 2D Brownian simulation
-(GPU Monte-Carlo, D drawn per 16 x 16 tile from U(0.2, 5) um^2/s,
+(tests/synth_host.c, D drawn per 16 x 16 tile from U(0.2, 5) um^2/s,
 single-exponential bleach tau = 20 s, 500 particles per 30 x 30 um, PSF
 1/e^2 radius 0.4 um, 10,000 photons/s per particle, offset 100), all-pixel
 multi-tau ACFs (P=16, Q=8, 73 channels) with blocked variance,
 single-exponential bleach correction, and a batched LM fit of the TIRF
-one-component model (N, D, G free) of every pixel.
+one-component model (N, D, G free) of every pixel.  Both arms read the same
+stack (same generator, same seed).
 
 One step = the whole path over the full stack.  `value` is measured with the
 stack resident in HBM (1.64 GB, larger than L2, so no flush is needed);
@@ -15,8 +16,12 @@ pinned host stack -> device, run, results -> host) every step.
 
 --impl reference runs the reference's CPU implementation of the path: the
 Java CPU code cannot run here (no JVM), so the FP64 C restatement in oracle/
-stands in for it, with all host threads (OpenMP), on a bounded sample of the
-same workload.
+stands in for it, with all host threads (OpenMP), on a bounded sample (a band
+of rows) of the same stack.
+
+The GPU arm also compares its outputs on the CPU-baseline sample with the
+oracle's (the `parity` block): blocking index and flag, fitted mask, ACF,
+blocked variance, fitted N and D.
 """
 from __future__ import annotations
 
@@ -68,12 +73,9 @@ def make_config(engine, lib):
                             cst=engine.model_constants(pixel_um=0.24, psf_um=0.4))
 
 
-def simulate_stack(engine, seed):
-    rng = np.random.default_rng(seed)
-    dmap = rng.uniform(0.2, 5.0, (H // 16, W // 16)).astype(np.float32)
-    return engine.simulate(W, H, T, frametime=1e-3, steps_per_frame=10, pixel_um=0.24, psf_um=0.4,
-                           density=500 / 900.0, cps=10000.0, tau_bleach=20.0, offset=100,
-                           margin=2.0, seed=seed, d_tile_map=dmap)
+def host_stack(seed):
+    from tests.synth import bench_stack
+    return bench_stack(W, H, T, seed=seed)
 
 
 class ClockSampler:
@@ -142,17 +144,52 @@ def load_profile_traffic():
 
 def cpu_baseline(stack_np, cfg, sample_pixels, threads):
     """The FP64 oracle (restatement of the Java CPU path) on a bounded sample
-    of the same workload: sample_pixels pixels of one row band, all frames."""
+    of the same workload: the first sample_pixels pixels (whole rows), all
+    frames.  Returns (pixels/s, pixels, seconds, oracle outputs)."""
     import oracle  # checker / baseline only
     ncols = min(sample_pixels, W)
     nrows = max(1, sample_pixels // ncols)
     sub = np.ascontiguousarray(stack_np[:, :nrows, :ncols])
     t0 = time.perf_counter()
-    oracle.run(sub, out_w=ncols, out_h=nrows, background=cfg.background, p=cfg.p, q=cfg.q,
-               frametime=cfg.frametime, bleach=cfg.bleach, init=np.array(cfg.init),
-               free_mask=np.array(cfg.free_mask, np.int32), cst=cfg.cst, threads=threads)
+    ref = oracle.run(sub, out_w=ncols, out_h=nrows, background=cfg.background, p=cfg.p, q=cfg.q,
+                     frametime=cfg.frametime, bleach=cfg.bleach, init=np.array(cfg.init),
+                     free_mask=np.array(cfg.free_mask, np.int32), cst=cfg.cst, threads=threads)
     dt = time.perf_counter() - t0
-    return ncols * nrows / dt, ncols * nrows, dt
+    return ncols * nrows / dt, ncols * nrows, dt, ref
+
+
+def parity_block(gpu, ref, n):
+    """GPU outputs of the first n pixels against the oracle's on the same pixels."""
+    g = {k: v[:n] for k, v in gpu.items()}
+    out = {"pixels": int(n)}
+    out["blocked_ind_equal"] = int((g["blocked_ind"] == ref["blocked_ind"]).sum())
+    out["blocked_ok_equal"] = int((g["blocked_ok"] == ref["blocked_ok"]).sum())
+    out["fitted_gpu"] = int(g["fitted"].sum())
+    out["fitted_oracle"] = int(ref["fitted"].sum())
+    out["fitted_equal"] = int((g["fitted"] == ref["fitted"]).sum())
+    fin_r = np.all(np.isfinite(ref["acf"][:, 1:]), axis=1)
+    fin_g = np.all(np.isfinite(g["acf"][:, 1:]), axis=1)
+    out["acf_all_lags_finite_oracle"] = int(fin_r.sum())
+    out["acf_finiteness_equal"] = int((np.isfinite(ref["acf"]) == np.isfinite(g["acf"])).all(axis=1).sum())
+    both = fin_r & fin_g
+    if both.any():
+        dev = np.abs(g["acf"][both, 1:] - ref["acf"][both, 1:]) / np.abs(ref["acf"][both, 1:2])
+        out["acf_max_dev_rel_g1"] = float(dev.max())
+        vr, vg = ref["var"][both, 1:], g["var"][both, 1:]
+        rel = np.abs(vg - vr) / np.abs(vr)
+        out["var_max_rel"] = float(rel.max())
+        out["var_median_rel"] = float(np.median(rel))
+    fb = (g["fitted"] == 1) & (ref["fitted"] == 1)
+    out["fitted_both"] = int(fb.sum())
+    if fb.any():
+        for i, name in ((0, "N"), (1, "D")):
+            e = np.abs(g["fitres"][fb, i] - ref["fitres"][fb, i]) / np.abs(ref["fitres"][fb, i])
+            out[f"{name}_max_rel"] = float(e.max())
+            out[f"{name}_over_1e-4"] = int((e > 1e-4).sum())
+        c = np.abs(g["chi2"][fb] - ref["chi2"][fb]) / np.abs(ref["chi2"][fb])
+        out["chi2_max_rel"] = float(c.max())
+    out["not_fitted_with_nonfinite_acf_oracle"] = int(((ref["fitted"] == 0) & ~fin_r).sum())
+    return out
 
 
 def reference_arm(args):
@@ -163,23 +200,22 @@ def reference_arm(args):
     oracle.build()
     threads = os.cpu_count() or 1
     from imaging_fcs_1_52_gb300 import engine, _lib  # configuration only
-    from tests.synth import brownian_stack
     cfg = make_config(engine, _lib)
     sample = args.cpu_sample or 1024
-    # the same simulation model and parameters on the host (numpy), one band
-    # of `sample` pixels x all frames
-    stack_np = brownian_stack(min(sample, W), max(1, sample // W), T, seed=1, tau_bleach=20.0)
+    stack_np = host_stack(seed=1)           # the GPU arm's stack (same generator, same seed)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, n, dt = cpu_baseline(stack_np, cfg, sample, threads)
+        v, n, dt, _ = cpu_baseline(stack_np, cfg, sample, threads)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sample / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": f"128x128x{T} uint16, single-exp bleach, P=16 Q=8, "
-                                            "OLS LM TIRF fit", "sample": f"{sample} pixels x {T} frames"},
+            "data": "synthetic (tests/synth_host.c, seed 1: the GPU arm's stack)",
+            "config": {"workload": f"128x128x{T} uint16 stack; single-exp bleach; P=16 Q=8 (73 ch); "
+                                   "blocked variance; OLS LM TIRF fit (N, D, G)",
+                       "sample": f"first {sample} pixels (rows 0..{sample // W - 1}) x {T} frames of that stack"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{sample} pixels x {T} frames, FP64 C restatement of the Java CPU path"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -200,7 +236,8 @@ def main():
     from imaging_fcs_1_52_gb300 import _lib, engine
 
     cfg = make_config(engine, _lib)
-    stack = simulate_stack(engine, seed=1 + rank)        # each rank: its own stack (weak scaling)
+    stack_np = host_stack(seed=1 + rank)                # each rank: its own stack (weak scaling)
+    stack = torch.from_numpy(stack_np.view(np.int16)).cuda().view(torch.uint16)
     torch.cuda.synchronize()
     plan = engine.Plan(cfg)
     plan.set_timing(True)
@@ -241,7 +278,7 @@ def main():
 
     # e2e through the C ABI with host buffers (pinned host stack)
     host = torch.empty((T, H, W), dtype=torch.int16, pin_memory=True)
-    host.copy_(stack.view(torch.int16).cpu())
+    host.copy_(torch.from_numpy(stack_np.view(np.int16)))
     host_np = host.numpy().view(np.uint16)
     outs_host = {}
     for n in engine.output_names(cfg):
@@ -270,19 +307,21 @@ def main():
         alg_bytes = T * H * W * 2 + cfg.npix * cfg.chanum * 8 * 2
         achieved = alg_bytes / (corr_avg * 1e-3) / 1e9
         sample = args.cpu_sample or 4096
-        stack_np = engine.to_numpy_u16(stack[:, :max(1, sample // W), :].contiguous())
-        cpu_v, cpu_n, cpu_dt = cpu_baseline(stack_np, cfg, sample, os.cpu_count() or 1)
+        cpu_v, cpu_n, cpu_dt, ref = cpu_baseline(stack_np, cfg, sample, os.cpu_count() or 1)
         # single-threaded, as the plugin's one worker thread runs it
-        cpu1_v, cpu1_n, cpu1_dt = cpu_baseline(stack_np, cfg, min(sample, 256), 1)
+        cpu1_v, cpu1_n, cpu1_dt, _ = cpu_baseline(stack_np, cfg, min(sample, 256), 1)
+        gpu_np = {k: v.cpu().numpy() for k, v in out.items()}
+        parity = parity_block(gpu_np, ref, cpu_n)
         fitted = int(out["fitted"].sum().item())
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU Monte-Carlo, seeded)",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (tests/synth_host.c, seeded; same stack as the reference arm)",
             "config": {"workload": f"128x128x{T} uint16 stack; single-exp bleach; P=16 Q=8 (73 ch); "
                                    "blocked variance; OLS LM TIRF fit (N, D, G)",
                        "pixels_per_rank": cfg.npix, "frames": T, "l2": f"stack {T * H * W * 2 / 1e9:.2f} GB > L2 (129 MB), no flush needed",
                        "parallelism": f"pixel shards x{world}", "fitted_pixels": fitted},
+            "fitted_pixels_per_s": world * fitted / (ms * 1e-3),
             "e2e": {"value": world * cfg.npix / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": launches,
@@ -298,6 +337,7 @@ def main():
             "cpu_baseline_single_thread": {"value": cpu1_v, "unit": UNIT, "cores": 1, "kind": "port",
                                            "sample": f"{cpu1_n} pixels x {T} frames, {cpu1_dt:.1f} s"},
             "clocks": clk.summary(),
+            "parity": parity,
         }
         print(json.dumps(line))
     if world > 1:

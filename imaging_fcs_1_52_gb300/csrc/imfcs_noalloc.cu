@@ -3,11 +3,12 @@
 // Same fit as imfcs_fit (Gpufit semantics, lm_kernel) but every argument is a
 // device pointer and the per-fit scratch (parameters in internal units, the
 // model constants, the fitted parameters) lives in a file-scope __device__
-// array of fixed size.  The array's address is resolved once per device with
-// cudaGetSymbolAddress; the call itself issues no cudaMalloc / cudaFree and no
+// array of fixed size.  The array's device address is looked up on every call
+// with cudaGetSymbolAddress in the caller's current context (a symbol's
+// address belongs to a context, so a cached address would go stale after a
+// cudaDeviceReset or in another context on the same device); the lookup
+// allocates nothing.  The call issues no cudaMalloc / cudaFree and no
 // allocating library routine.
-#include <mutex>
-
 #include "imfcs_args.h"
 #include "imfcs_host.h"
 
@@ -18,12 +19,6 @@ cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream);
 // Per fit: init (11) + constants (9) + fitted parameters (11) floats.
 constexpr int kNoAllocPerFit = IMFCS_NPARAM + IMFCS_NCONST + IMFCS_NPARAM;
 static __device__ __align__(256) float g_noalloc_scratch[(size_t)IMFCS_FIT_NOALLOC_MAX_FITS * kNoAllocPerFit];
-
-constexpr int kMaxDevices = 64;
-static float *g_scratch_ptr[kMaxDevices];
-static int g_sms[kMaxDevices];
-static std::once_flag g_once[kMaxDevices];
-static cudaError_t g_setup_rc[kMaxDevices];
 
 // Internal-unit initial values and per-fit constants from the caller's
 // [fit][nparam] array (ACF_1D: SI units, constants at 11..19).
@@ -88,22 +83,21 @@ extern "C" int imfcs_fit_device_noalloc(int n_fits, int n_points, const float *d
         return -1;
     }
     if (n_fits == 0) return 0;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    // Errors left on this thread by earlier, unrelated work are reported as
+    // such instead of being attributed to the launches below.
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error(cuda_msg(e, "error pending before imfcs_fit_device_noalloc")); return -1; }
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) { set_error(cuda_msg(e, "cudaGetDevice")); return -1; }
-    if (dev < 0 || dev >= kMaxDevices) { set_error("device index out of range"); return -1; }
-    // once per device: the scratch array's address and the SM count
-    std::call_once(g_once[dev], [dev] {
-        g_setup_rc[dev] = cudaGetSymbolAddress((void **)&g_scratch_ptr[dev], g_noalloc_scratch);
-        if (g_setup_rc[dev] == cudaSuccess)
-            g_setup_rc[dev] = cudaDeviceGetAttribute(&g_sms[dev], cudaDevAttrMultiProcessorCount, dev);
-    });
-    if (g_setup_rc[dev] != cudaSuccess) {
-        set_error(cuda_msg(g_setup_rc[dev], "cudaGetSymbolAddress(scratch)"));
-        return -1;
-    }
+    // the scratch array's address in the current context, and the SM count
+    float *scratch = nullptr;
+    e = cudaGetSymbolAddress((void **)&scratch, g_noalloc_scratch);
+    if (e != cudaSuccess) { set_error(cuda_msg(e, "cudaGetSymbolAddress(scratch)")); return -1; }
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { set_error(cuda_msg(e, "cudaDeviceGetAttribute(SM count)")); return -1; }
     cudaStream_t s = (cudaStream_t)stream;
-    float *init_int = g_scratch_ptr[dev];
+    float *init_int = scratch;
     float *cst = init_int + (size_t)IMFCS_FIT_NOALLOC_MAX_FITS * IMFCS_NPARAM;
     float *par = cst + (size_t)IMFCS_FIT_NOALLOC_MAX_FITS * IMFCS_NCONST;
 
@@ -133,7 +127,7 @@ extern "C" int imfcs_fit_device_noalloc(int n_fits, int n_points, const float *d
     a.out_chi2 = output_chi_squares;
     a.out_state = output_states;
     a.out_iter = output_n_iterations;
-    e = launch_lm(a, g_sms[dev], s);
+    e = launch_lm(a, sms, s);
     if (e != cudaSuccess) { set_error(cuda_msg(e, "lm_kernel")); return -1; }
 
     noalloc_finish_kernel<<<blocks, threads, 0, s>>>(n_fits, nparam, np, acf, initial_parameters, par,

@@ -32,7 +32,11 @@ def diffusion_partials(fitres: np.ndarray, fitted: np.ndarray) -> np.ndarray:
 
 
 def diffusion_point(partials: np.ndarray) -> tuple[float, float]:
-    """Mean D [um^2/s] and variance of D from reduced partials (java:11189-11191)."""
+    """Mean D [um^2/s] and variance of D from reduced partials (java:11189-11191).
+    A binning without a fitted pixel gives (nan, nan), as the reference's
+    0/0 does (java:11187-11189)."""
     n, s, s2 = partials
+    if n == 0:
+        return float("nan"), float("nan")
     mean = s * 1e12 / n
     return mean, s2 * 1e24 / n - mean * mean

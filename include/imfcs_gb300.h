@@ -7,8 +7,8 @@
  * libagpufit.so (agpufitjni.cu).  Every reference-facing entry point below
  * names the Java native method and the agpufitjni.cu implementation it
  * replaces.  Plain C types only: pointers, sizes and the two parameter
- * structs.  A JNI shim that forwards the Java natives to these functions is
- * given in INTEGRATION.md.
+ * structs.  A JNI shim (jni/imfcs_jni.c in this repository) forwards the
+ * Java natives to these functions.
  *
  * Conventions
  *  - Return value: 0 = success, nonzero = error; imfcs_get_last_error()
@@ -129,7 +129,9 @@ IMFCS_API int imfcs_is_acf_memory_sufficient(const imfcs_acf_parameters *p);
  * flag).  bleachcorr_params[h_temp][w_temp][bleachcorr_order] are polynomial
  * coefficients in powers of t (seconds) when bleachcorr_gpu != 0.  samp and
  * lag receive the lag tables.  Semantics follow the plugin's Java CPU
- * correlator (java:9124-9648), see the design doc. */
+ * correlator (java:9124-9648): time origin (x + 0.5) with 1-based x, the
+ * averaged trace in int division, the zero-led lag-1 sequence of the
+ * blocking transform. */
 IMFCS_API int imfcs_calc_acf(const float *pixels, double *pixels1, double *blockvararray,
                    double *NBmean, double *NBcov, double *blocked1D,
                    const double *bleachcorr_params, double *samp, int *lag,
@@ -161,8 +163,9 @@ IMFCS_API int imfcs_fit(int n_fits, int n_points, const float *data, const float
  * file-scope device array sized for IMFCS_FIT_NOALLOC_MAX_FITS fits (2 MB);
  * larger batches are rejected with an error (split them).  No part of the
  * scratch needs to start at zero: each call writes every element it reads.
- * The first call on a device resolves the scratch address
- * (cudaGetSymbolAddress) and should precede any stream capture.  Calls that
+ * Every call looks up the scratch address in the current context
+ * (cudaGetSymbolAddress, which allocates nothing), so the entry point stays
+ * valid after a cudaDeviceReset or in another context.  Calls that
  * overlap on one device (other host threads or streams) share the scratch
  * and race: serialise them.  Returns 0 / -1 (imfcs_get_last_error). */
 #define IMFCS_FIT_NOALLOC_MAX_FITS 16384

@@ -101,7 +101,7 @@ def _declare(L):
     L.imfcs_o_line_fit.argtypes = [_dp, _dp, _dp, C.c_int, _dp]
     L.imfcs_o_run.restype = C.c_int
     L.imfcs_o_run.argtypes = [C.POINTER(Config), _u16p, C.c_void_p, _dp, _dp, _dp, _ip, _ip,
-                              _dp, _dp, _ip, C.c_void_p]
+                              _dp, _dp, _ip, C.c_void_p, C.c_void_p]
 
 
 # ----------------------------------------------------------------------------- helpers
@@ -312,8 +312,12 @@ def run(stack, *, out_w, out_h, map_x0=0, map_y0=0, binx=1, biny=1, pixbinx=None
     chi2 = np.full(n, np.nan)
     fitted = np.zeros(n, np.int32)
     prob = np.zeros((n, 2))
+    covmats = np.zeros((n, c - 1, c - 1)) if gls else None
     bgr_p = None if bgr is None else np.ascontiguousarray(bgr, np.int32).ctypes.data
     lib().imfcs_o_run(C.byref(cfg), stack, bgr_p, acf, var, sd, bind, bok, fitres, chi2, fitted,
-                      prob.ctypes.data if bayes else None)
-    return dict(acf=acf, var=var, sd=sd, blocked_ind=bind, blocked_ok=bok, fitres=fitres,
-                chi2=chi2, fitted=fitted, bayes_prob=prob)
+                      prob.ctypes.data if bayes else None, None if covmats is None else covmats.ctypes.data)
+    out = dict(acf=acf, var=var, sd=sd, blocked_ind=bind, blocked_ok=bok, fitres=fitres,
+               chi2=chi2, fitted=fitted, bayes_prob=prob)
+    if covmats is not None:
+        out["covmats"] = covmats
+    return out

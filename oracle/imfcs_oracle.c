@@ -1048,7 +1048,7 @@ int imfcs_o_line_fit(const double *x, const double *y, const double *sd, int n, 
 /* ------------------------------------------------------------------------ */
 int imfcs_o_run(const imfcs_o_config *cfg, const uint16_t *stack, const int *bgr, double *acf,
                 double *var, double *sd, int *blocked_ind, int *blocked_ok, double *fitres,
-                double *chi2, int *fitted, double *bayes_prob)
+                double *chi2, int *fitted, double *bayes_prob, double *covmats)
 {
     const int chanum = imfcs_o_chanum(cfg->p, cfg->q);
     const int num = cfg->num;
@@ -1099,6 +1099,9 @@ int imfcs_o_run(const imfcs_o_config *cfg, const uint16_t *stack, const int *bgr
         imfcs_o_calculate_cf(c0, c1, num, ind, cfg->p, cfg->q, lag, samp, mtab, cfg->gls, a, v, s, covm);
         blocked_ind[pix] = ind;
         blocked_ok[pix] = bok;
+        if (covm && covmats)
+            memcpy(covmats + (size_t)pix * (chanum - 1) * (chanum - 1), covm,
+                   sizeof(double) * (chanum - 1) * (chanum - 1));
         if (cfg->do_fit) {
             double *fr = fitres + (size_t)pix * IMFCS_O_NPARAM, x2 = NAN;
             int st;

@@ -132,7 +132,8 @@ typedef struct {
 
 int imfcs_o_run(const imfcs_o_config *cfg, const uint16_t *stack, const int *bgr,
                 double *acf, double *var, double *sd, int *blocked_ind, int *blocked_ok,
-                double *fitres, double *chi2, int *fitted, double *bayes_prob);
+                double *fitres, double *chi2, int *fitted, double *bayes_prob,
+                double *covmats /* [pixel][(chanum-1)^2] when gls, nullable */);
 
 #ifdef __cplusplus
 }

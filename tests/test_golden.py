@@ -74,4 +74,4 @@ def test_gpu_matches_golden(name):
     assert both.sum() >= 0.95 * (d["fitted"] == 1).sum()
     for i in (0, 1):
         err = np.abs(g["fitres"][both, i] - d["fitres"][both, i]) / np.abs(d["fitres"][both, i])
-        assert np.median(err) <= FIT_TOL
+        assert err.max() <= FIT_TOL

@@ -49,12 +49,14 @@ def check_acf(gpu, ref):
 @pytest.mark.parametrize("kw", [
     {},
     {"q": 6},
+    {"q": 4},
+    {"q": 3, "cfx": 1, "cfy": 1},
     {"binx": 2, "biny": 2},
     {"binx": 3, "biny": 2, "pixbinx": 1, "pixbiny": 1},
     {"cfx": 1, "cfy": 0},
     {"cfx": 0, "cfy": 2},
     {"cfx": 2, "cfy": 1},
-], ids=["acf", "q6", "bin2", "bin3x2-overlap", "ccf10", "ccf02", "ccf21"])
+], ids=["acf", "q6", "q4", "q3-ccf11", "bin2", "bin3x2-overlap", "ccf10", "ccf02", "ccf21"])
 def test_correlator_no_bleach(dim_stack, kw):
     cfg = engine.FCSConfig(width=8, height=8, frames=4000, background=100, do_fit=False, **kw)
     gpu, ref = run_both(dim_stack, cfg)

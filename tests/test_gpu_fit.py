@@ -57,7 +57,14 @@ def test_gls_fit_parity(bright):
     np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
     both, errs = fit_errors(gpu, ref)
     assert both.sum() >= 32
-    assert np.median(errs[1]) <= FIT_TOL
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+    # the regularised covariance the fit whitens with (java:9524-9610), per
+    # pixel relative to its largest element
+    cg, cr = gpu["covmats"], ref["covmats"]
+    fin = np.all(np.isfinite(cr.reshape(len(cr), -1)), axis=1)
+    assert fin.sum() >= 32
+    scale = np.abs(cr[fin]).reshape(fin.sum(), -1).max(axis=1)[:, None, None]
+    assert np.max(np.abs(cg[fin] - cr[fin]) / scale) <= 1e-4
 
 
 @pytest.fixture(scope="module")
@@ -80,9 +87,11 @@ def test_bayes_probabilities(two_species):
     ok = ok_r & ok_g
     assert ok.sum() >= 32
     np.testing.assert_allclose(p_g[ok].sum(1), 1.0, atol=1e-5)
-    # same model choice on every pixel where the reference is decisive
+    # same model choice on every pixel where the reference is decisive, and
+    # the probabilities themselves
     dec = ok & (np.abs(p_r[:, 0] - 0.5) > 0.01)
     np.testing.assert_array_equal(p_g[dec, 0] > 0.5, p_r[dec, 0] > 0.5)
+    assert np.max(np.abs(p_g[ok] - p_r[ok])) <= 1e-3
 
 
 def _acf_curves(nfits, seed=0):
@@ -241,8 +250,8 @@ def test_diffusion_law():
         d = r["fitres"][r["fitted"] == 1, 1]
         mean, var = d.mean() * 1e12, (d ** 2).mean() * 1e24 - (d.mean() * 1e12) ** 2
         assert abs(out[3 * (u - 1)] - cst[6] * 1e12) <= 1e-9 * out[3 * (u - 1)]
-        assert abs(out[3 * (u - 1) + 1] - mean) <= 1e-3 * mean
-        assert abs(out[3 * (u - 1) + 2] - var) <= 1e-2 * abs(var) + 1e-6
+        assert abs(out[3 * (u - 1) + 1] - mean) <= 1e-4 * mean
+        assert abs(out[3 * (u - 1) + 2] - var) <= 1e-3 * abs(var) + 1e-6
     x = out[0::3]
     yv = x / out[1::3]
     sd = x / out[1::3] ** 2 * np.sqrt(out[2::3])
@@ -258,3 +267,120 @@ def test_simulator_is_seeded_and_bleaches():
     m = a.view(torch.int16).float().mean(dim=(1, 2)).cpu().numpy() - 100
     early, late = m[:300].mean(), m[-300:].mean()
     assert late < early * np.exp(-2.4) * 1.5   # ~exp(-t/tau) emission over 3 s
+
+
+# ---------------------------------------------------------------------------
+# FCS_3p model terms beyond the one-component TIRF case, through the
+# reference fit API (Gpufit ACF_1D) against the oracle's standardFit: SPIM
+# (finite sz), flow (vx, vy), triplet, a second and a third component, and
+# the cross-correlation distance terms (rx, ry).
+# ---------------------------------------------------------------------------
+def _model_case(par, cst, free, init, nfits=12, seed=0, rel_noise=0.002):
+    lag, _, _ = oracle.lag_tables(16, 8, 50000)
+    lagtime = lag * 1e-3
+    rng = np.random.default_rng(seed)
+    data, var = [], []
+    for i in range(nfits):
+        p = np.array(par, float)
+        p[0] *= rng.uniform(0.8, 1.25)
+        p[1] *= rng.uniform(0.8, 1.25)
+        g = np.array([oracle.fcs_model(p, cst, t) for t in lagtime])
+        sd = rel_noise * np.abs(g[1]) + 0.01 * np.abs(g - p[4])
+        data.append(g + rng.normal(0, 1, g.size) * sd)
+        var.append(sd ** 2)
+    return np.array(data), np.array(var), lagtime
+
+
+def _fit_api_vs_oracle(par, cst, free, init, **kw):
+    L = _lib.load()
+    data, var, lagtime = _model_case(par, cst, free, init, **kw)
+    n, npts = len(data), len(lagtime) - 1
+    y = np.ascontiguousarray(data[:, 1:], np.float32)
+    w = np.ascontiguousarray(1.0 / var[:, 1:], np.float32)
+    ini = np.zeros((n, 20), np.float32)
+    ini[:, :11] = init
+    ini[:, 11:20] = cst
+    ptf = np.zeros(20, np.int32)
+    ptf[:11] = free
+    ui = np.ascontiguousarray(lagtime[1:], np.float32)
+    outp = np.zeros((n, 20), np.float32)
+    st = np.zeros(n, np.int32)
+    chi = np.zeros(n, np.float32)
+    rc = L.imfcs_fit(n, npts, y.ctypes.data, w.ctypes.data, 2, ini.ctypes.data, C.c_float(1e-16), 2000, 0,
+                     ptf.ctypes.data, 0, ui.nbytes, ui.ctypes.data, outp.ctypes.data, st.ctypes.data,
+                     chi.ctypes.data, None)
+    assert rc == 0, _lib.last_error()
+    idx = np.flatnonzero(free)
+    checked = 0
+    for i in range(n):
+        r = oracle.fit_ols(data[i], var[i], lagtime, 1, npts, np.array(init, float),
+                           np.array(free, np.int32), cst)
+        if r["status"] != 0:
+            continue
+        assert st[i] == 0
+        for j in idx:
+            # FIT_TOL relative, or 1e-4 of the parameter's standard error where
+            # the fitted value is near zero (flow components)
+            tol = max(FIT_TOL * abs(r["params"][j]), 1e-4 * r["sigma"][list(idx).index(j)])
+            assert abs(outp[i, j] - r["params"][j]) <= tol, (i, j, outp[i, j], r["params"][j])
+        assert abs(chi[i] - r["chi2"] * (npts - len(idx) - 1)) <= 1e-3 * chi[i]
+        checked += 1
+    assert checked >= n // 2
+    return checked
+
+
+def _cst(sz=1e6 * 0.515 / 1.49 * 1e-6, rx=0.0, ry=0.0, q2=1.0, q3=1.0, s=0.4e-6):
+    ax = ay = 0.24e-6
+    return np.array([ax, ay, s, sz, rx, ry, oracle.obsvol(ax, ay, s), q2, q3])
+
+
+ONE = [1, 1, 0, 0, 1, 0, 0, 0, 0, 0, 0]
+
+
+def test_model_spim_finite_sz():
+    par = [5.0, 2e-12, 0, 0, 0.001, 0, 0, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(sz=0.9e-6), ONE, [1, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0, 0])
+
+
+def test_model_flow_vx_vy():
+    par = [5.0, 1e-12, 4e-5, -2e-5, 0.001, 0, 0, 0, 0, 0, 0]
+    free = [1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(), free, [4, 1.2e-12, 3e-5, -1e-5, 0, 0, 0, 0, 0, 0, 0], rel_noise=0.001)
+
+
+def test_model_triplet_held_and_free():
+    par = [5.0, 2e-12, 0, 0, 0.001, 0, 0, 0, 0, 0.25, 2e-5]
+    held = [1.0, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0.25, 2e-5]
+    _fit_api_vs_oracle(par, _cst(), ONE, held)
+    free = [1, 1, 0, 0, 1, 0, 0, 0, 0, 1, 1]
+    _fit_api_vs_oracle(par, _cst(), free, [4, 1.5e-12, 0, 0, 0, 0, 0, 0, 0, 0.2, 3e-5], rel_noise=0.0005)
+
+
+def test_model_two_components():
+    par = [5.0, 0.5e-12, 0, 0, 0.001, 0.3, 8e-12, 0, 0, 0, 0]
+    free = [1, 1, 0, 0, 1, 1, 1, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(), free, [4, 0.6e-12, 0, 0, 0, 0.25, 6e-12, 0, 0, 0, 0], rel_noise=0.0005)
+
+
+def test_model_third_component_and_brightness():
+    par = [5.0, 0.5e-12, 0, 0, 0.001, 0.3, 5e-12, 0.2, 30e-12, 0, 0]
+    held = [1, 1e-12, 0, 0, 0, 0.3, 5e-12, 0.2, 30e-12, 0, 0]
+    _fit_api_vs_oracle(par, _cst(q2=1.5, q3=0.8), ONE, held)
+
+
+def test_model_cross_correlation_distance():
+    # the spatial CCF model at a one-pixel distance in x and in x and y
+    par = [5.0, 3e-12, 0, 0, 0.0, 0, 0, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(rx=0.24e-6), ONE, [4, 2e-12, 0, 0, 0, 0, 0, 0, 0, 0, 0])
+    _fit_api_vs_oracle(par, _cst(rx=0.24e-6, ry=0.24e-6), ONE, [4, 2e-12, 0, 0, 0, 0, 0, 0, 0, 0, 0])
+
+
+def test_plan_spim_fit_on_a_stack(bright):
+    """The whole path with SPIM constants (finite sz) on a correlated stack."""
+    cst = engine.model_constants(sz_um=0.9)
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000, background=100, cst=cst)
+    gpu, ref = run_both(bright, cfg)
+    np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 48
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL

@@ -23,6 +23,11 @@ def test_shard_rows_cover_exactly():
             assert [s for s, _ in rows] == list(np.cumsum([0] + [n for _, n in rows[:-1]]))
 
 
+def test_diffusion_point_of_empty_binning_is_nan():
+    mean, var = shard.diffusion_point(shard.diffusion_partials(np.zeros((4, 11)), np.zeros(4, np.int32)))
+    assert np.isnan(mean) and np.isnan(var)
+
+
 def _worker(rank, world, port, stack, q):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)

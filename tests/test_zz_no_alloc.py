@@ -1,6 +1,8 @@
 """imfcs_fit_device_noalloc: the fit on device buffers with file-scope
-scratch.  Compared with imfcs_fit (host buffers, allocating) on the same
-inputs, on two calls in a row.  Collected last on purpose."""
+scratch, for callers that cannot allocate device memory at fit time.
+Compared with imfcs_fit (host buffers, allocating) on the same inputs, on two
+calls in a row, at a small batch and at exactly the maximum batch; a warm call
+must leave the device's free memory unchanged.  Collected last on purpose."""
 import ctypes as C
 
 import numpy as np
@@ -101,3 +103,53 @@ def test_noalloc_linear_fit_matches_allocating_fit():
             f_g = np.polynomial.polynomial.polyval(x.astype(float), got[i, :ncoef].astype(float))
             f_r = np.polynomial.polynomial.polyval(x.astype(float), outp[i, :ncoef].astype(float))
             assert np.max(np.abs(f_g - f_r)) <= 1e-5 * np.abs(f_r).max()
+
+
+def _fit_inputs(n):
+    base, var, lagtime, cst = _acf_curves(64, seed=5)
+    reps = (n + 63) // 64
+    data = np.tile(base, (reps, 1))[:n]
+    var = np.tile(var, (reps, 1))[:n]
+    y = np.ascontiguousarray(data[:, 1:], np.float32)
+    w = np.ascontiguousarray(1.0 / var[:, 1:], np.float32)
+    init = np.zeros((n, 20), np.float32)
+    init[:, 0], init[:, 1] = 1.0, 1e-12
+    init[:, 11:20] = cst
+    x = np.ascontiguousarray(lagtime[1:], np.float32)
+    return y, w, init, x
+
+
+@pytest.mark.gpu
+def test_noalloc_at_maximum_batch_allocates_nothing():
+    import torch
+    L = _lib.load()
+    n, npts = 16384, 72                      # == IMFCS_FIT_NOALLOC_MAX_FITS
+    y, w, init, x = _fit_inputs(n)
+    ptf = np.zeros(20, np.int32)
+    ptf[[0, 1, 4]] = 1
+    outp = np.zeros((n, 20), np.float32)
+    st = np.zeros(n, np.int32)
+    rc = L.imfcs_fit(n, npts, y.ctypes.data, w.ctypes.data, 2, init.ctypes.data, C.c_float(1e-16), 2000, 0,
+                     ptf.ctypes.data, 0, x.nbytes, x.ctypes.data, outp.ctypes.data, st.ctypes.data, None, None)
+    assert rc == 0, _lib.last_error()
+    dev = torch.device("cuda:0")
+    d_y, d_w, d_init, d_x = (torch.from_numpy(a).to(dev) for a in (y, w, init, x))
+    d_out = torch.full((n, 20), float("nan"), device=dev)
+    d_st = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = L.imfcs_fit_device_noalloc(n, npts, d_y.data_ptr(), d_w.data_ptr(), 2, d_init.data_ptr(),
+                                        C.c_float(1e-16), 2000, 0, ptf.ctypes.data, d_x.data_ptr(),
+                                        d_out.data_ptr(), d_st.data_ptr(), None, None,
+                                        C.c_void_p(stream.cuda_stream))
+        assert rc == 0, _lib.last_error()
+        torch.cuda.synchronize()
+
+    call()                                   # warm: module loading happens here
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    assert torch.cuda.mem_get_info()[0] == free0
+    np.testing.assert_array_equal(d_st.cpu().numpy(), st)
+    got = d_out.cpu().numpy()
+    np.testing.assert_allclose(got[:, [0, 1, 4]], outp[:, [0, 1, 4]], rtol=FIT_TOL, atol=1e-7)
