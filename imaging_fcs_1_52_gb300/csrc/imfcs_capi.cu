@@ -237,10 +237,11 @@ struct imfcs_plan {
     double *proj = nullptr;
     int *snap_pos = nullptr;
     float2 *segtot = nullptr, *snap_part = nullptr;
+    int *segbad = nullptr, *snap_bad = nullptr;   // non-finite frames per segment / snapshot partial
     float4 *mon = nullptr, *blkmon = nullptr;
     float *s1 = nullptr, *s2 = nullptr, *segsum = nullptr;
     int *blk_ind = nullptr, *blk_ok = nullptr;
-    float *stats = nullptr, *bprod = nullptr, *streams = nullptr;
+    float *stats = nullptr, *bprod = nullptr, *streams = nullptr, *s0 = nullptr;
     float *linv = nullptr, *ytrans = nullptr;
     int *gls_ok = nullptr;
     float *fit_y = nullptr, *fit_w = nullptr, *fit_x = nullptr, *fit_x_gls = nullptr;
@@ -392,6 +393,8 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     AL(pl->snap_pos, kMaxSnap);
     AL(pl->segtot, nt * pl->nseg);
     AL(pl->snap_part, nt * j.nsnap);
+    AL(pl->segbad, nt * pl->nseg);
+    AL(pl->snap_bad, nt * j.nsnap);
     AL(pl->mon, np * chanum);
     AL(pl->blkmon, np);
     AL(pl->s1, np * pl->nbseg * (kBlkSegLog + 1));
@@ -401,6 +404,7 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     AL(pl->blk_ok, np);
     AL(pl->stats, corr_stats_floats(j));
     AL(pl->streams, corr_stream_floats(j));
+    AL(pl->s0, level0_stream_floats(j));
     AL(pl->acf_int, np * chanum);
     AL(pl->var_int, np * chanum);
     AL(pl->lagtime, chanum);
@@ -576,15 +580,18 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     else CK(launch_bleach(j, pl->trace, pl->proj, (float)pl->uscale, (float)pl->uoff, pl->bparams, s));
     pl->launches += 2;
     pl->mark(1, s);
-    CK(launch_monitor(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->snap_pos, pl->nseg,
-                      pl->segtot, pl->snap_part, pl->mon, pl->blkmon, s));
+    // one streaming pass over the raw stack: the corrected, centred level-0
+    // stream and the monitor partial sums
+    CK(launch_stream(j, dev_stack, pl->bparams, pl->basis, pl->snap_pos, pl->nseg, pl->s0, pl->segtot,
+                     pl->snap_part, pl->segbad, pl->snap_bad, pl->dev_err, s));
+    CK(launch_monitor_finalize(j, pl->li_dev, pl->bparams, pl->nseg, pl->segtot, pl->snap_part, pl->segbad,
+                               pl->snap_bad, pl->mon, pl->blkmon, s));
     pl->launches += 2;
     pl->mark(2, s);
-    CK(launch_block(j, dev_stack, pl->bparams, pl->basis, pl->blkmon, pl->nbseg, pl->s1, pl->s2,
-                    pl->segsum, pl->blk_ind, pl->blk_ok, s));
+    CK(launch_block(j, pl->s0, pl->blkmon, pl->nbseg, pl->s1, pl->s2, pl->segsum, pl->blk_ind, pl->blk_ok, s));
     pl->launches += 2;
     pl->mark(3, s);
-    CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->mon, pl->blk_ind, acf, var,
+    CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->s0, pl->mon, pl->blk_ind, acf, var,
                    dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats, pl->streams,
                    c.gls, pl->dev_err, s));
     pl->launches += corr_kernel_count(j);

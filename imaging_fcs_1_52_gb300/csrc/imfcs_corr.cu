@@ -29,6 +29,7 @@
 #include <string.h>
 
 #include "imfcs_corr.cuh"
+#include "imfcs_tma.cuh"
 
 namespace imfcs {
 
@@ -223,46 +224,6 @@ __host__ __device__ inline size_t corr_smem_floats_dev(int q, bool ccf)
 // loaded by one thread while the CTA correlates the previous chunk.  Waits
 // are bounded: on a timeout the CTA records an error and leaves.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void tma_load_box(const CUtensorMap *tmap, void *dst, uint64_t *mbar, int x, int y,
-                                             int t, uint32_t bytes)
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
-                 : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(t), "r"(smem_u32(mbar))
-        : "memory");
-}
-
-// Bounded wait on an mbarrier phase.  Returns false after ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
-{
-    const uint32_t a = smem_u32(mbar);
-    for (int i = 0; i < (1 << 20); i++) {
-        uint32_t done;
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(a), "r"(parity), "r"(1000)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
 // Window value of a trace from the staged raw tile (frame fr of the chunk).
 __device__ __forceinline__ float tile_value(const Job &j, const uint16_t *tile, int BW, int BH, int fr, int xr, int yr)
 {
@@ -400,8 +361,10 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
                         vb -= bpb[12];
                     }
                 }
-                buf0[(kHist + fr) * 32 + lane] = va;
-                if (CCF) buf1[(kHist + fr) * 32 + lane] = vb;
+                // non-finite frames enter as 0: the monitors make exactly the
+                // lags whose windows hold one non-finite
+                buf0[(kHist + fr) * 32 + lane] = isfinite(va) ? va : 0.f;
+                if (CCF) buf1[(kHist + fr) * 32 + lane] = isfinite(vb) ? vb : 0.f;
             }
         } else {
             for (int i = tid; i < kChunk * 32; i += kCorrThreads) {
@@ -581,9 +544,8 @@ template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, c
 // kernel covers the rest (blocks shorter than 16 samples).
 // ---------------------------------------------------------------------------
 bool corr2_supported(const Job &j);
-cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
-                         const float *basis, const float4 *mon, const int *blk_ind, const CorrOut &o,
-                         float *streams, cudaStream_t stream);
+cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
+                         const CorrOut &o, float *streams, cudaStream_t stream);
 
 size_t corr_smem_bytes(int q, bool ccf) { return corr_smem_floats_dev(q, ccf) * sizeof(float); }
 
@@ -608,16 +570,8 @@ static TmaGeom tma_geometry(const Job &j, const void *stack)
 
 static bool encode_stack_map(const Job &j, const void *stack, const TmaGeom &g, CUtensorMap *map)
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess || !p)
-            return false;
-        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+    if (!fn) return false;
     const int frames_total = j.first + j.num;
     cuuint64_t dims[3] = {(cuuint64_t)j.in_w, (cuuint64_t)j.in_h, (cuuint64_t)frames_total};
     cuuint64_t strides[2] = {(cuuint64_t)j.in_w * 2, (cuuint64_t)j.in_w * j.in_h * 2};
@@ -630,7 +584,7 @@ static bool encode_stack_map(const Job &j, const void *stack, const TmaGeom &g, 
 }
 
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
-                        const float *basis, const float4 *mon, const int *blk_ind, double *acf,
+                        const float *basis, const float *s0, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
                         int pnum_stride, float *stats, float *streams, int gls, int *err,
                         cudaStream_t stream)
@@ -638,7 +592,7 @@ cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, cons
     CorrOut o;
     o.acf = acf; o.var = var; o.sd = sd; o.nb_mean = nb_mean; o.nb_cov = nb_cov;
     o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls; o.err = err;
-    if (corr2_supported(j)) return launch_corr2(j, li, stack, bparams, basis, mon, blk_ind, o, streams, stream);
+    if (corr2_supported(j)) return launch_corr2(j, li, s0, mon, blk_ind, o, streams, stream);
     TmaGeom g = tma_geometry(j, stack);
     CUtensorMap map;
     memset(&map, 0, sizeof(map));

@@ -34,7 +34,6 @@
 namespace imfcs {
 
 constexpr int kC2Threads = 64;
-constexpr int kVFrames = 256;                // frames per thread in the values pass
 constexpr int kHeadFields = (kP + 1) + 8;                   // first-level heads d = 0..16, second-level d = 9..16
 
 // Arguments shared by the pair, tail and finalise kernels.
@@ -56,34 +55,56 @@ struct C2Ctx {
     float *bprod;
     int npix, pix, chanum, pnum_stride, gls;
     int ind, pnum, zfirst;
+    bool valid;               // false: a lane without a pixel (computes, writes nothing)
+    // where the block statistics of this (pixel, segment) live: the global
+    // array (stride npix) or a shared-memory copy (stride = threads) that the
+    // caller writes back; and (optional) the lags' monitors (a, b) in shared
+    // memory with stride smon_stride, both from lag lag0 on
+    float *sst;
+    int sst_stride;
+    const float2 *smon;
+    int smon_stride;
+    int lag0;
+    __device__ __forceinline__ float &stat(int lag, int s) const
+    {
+        return sst[(size_t)((lag - lag0) * kStatN + s) * sst_stride];
+    }
+    __device__ __forceinline__ float2 monitor(int lag) const
+    {
+        if (smon) return smon[(lag - lag0) * smon_stride];
+        const float4 m = __ldg(&mon[lag]);
+        return make_float2(m.x, m.y);
+    }
 };
 
 // One block end of one lag: total, blocked product and its statistics.
 __device__ __forceinline__ void c2_block_stat(const C2Ctx &c, int lag, float A, float B0, float D, int L, int z)
 {
-    const float4 m = __ldg(&c.mon[lag]);
+    if (!c.valid) return;
+    const float2 m = c.monitor(lag);
     const float a = m.x, b = m.y;
     const float P = (A - b * B0 - a * D + (float)L * a * b) / (float)L;
-    float &ahi = stat_ref(c.stats, c.npix, lag, 0, c.pix);
-    float &alo = stat_ref(c.stats, c.npix, lag, 1, c.pix);
+    float &ahi = c.stat(lag, 0);
+    float &alo = c.stat(lag, 1);
     ff t = {ahi, alo};
     ff_add(t, A);
     ahi = t.hi;
     alo = t.lo;
     if (z < c.pnum) {
-        float &r = stat_ref(c.stats, c.npix, lag, 4, c.pix);
+        float &r = c.stat(lag, 4);
         if (z == c.zfirst) r = P;      // per-segment shift of the block statistics
         const float dv = P - r;
-        stat_ref(c.stats, c.npix, lag, 2, c.pix) += dv;
-        stat_ref(c.stats, c.npix, lag, 3, c.pix) += dv * dv;
+        c.stat(lag, 2) += dv;
+        c.stat(lag, 3) += dv * dv;
         if (c.gls && lag >= 1) c.bprod[((size_t)c.pix * (c.chanum - 1) + (lag - 1)) * c.pnum_stride + z] = P;
     }
 }
 
 __device__ __forceinline__ void c2_add_total(const C2Ctx &c, int lag, float A)
 {
-    float &ahi = stat_ref(c.stats, c.npix, lag, 0, c.pix);
-    float &alo = stat_ref(c.stats, c.npix, lag, 1, c.pix);
+    if (!c.valid) return;
+    float &ahi = c.stat(lag, 0);
+    float &alo = c.stat(lag, 1);
     ff t = {ahi, alo};
     ff_add(t, A);
     ahi = t.hi;
@@ -92,6 +113,8 @@ __device__ __forceinline__ void c2_add_total(const C2Ctx &c, int lag, float A)
 
 __device__ __forceinline__ void c2_ctx(C2Ctx &c, const C2Args &a, int pix, int seg, int k)
 {
+    c.valid = pix < a.npix;
+    if (!c.valid) pix = a.npix - 1;   // reads stay in bounds; writes are masked
     c.stats = a.o.stats + (size_t)seg * a.stat_stride;
     c.mon = a.mon + (size_t)pix * a.chanum;
     c.bprod = a.o.bprod;
@@ -103,45 +126,11 @@ __device__ __forceinline__ void c2_ctx(C2Ctx &c, const C2Args &a, int pix, int s
     c.ind = a.blk_ind[pix];
     c.pnum = a.li->pnum_by_ind[c.ind];
     c.zfirst = (seg << a.seg_log[k]) >> c.ind;
-}
-
-// ---------------------------------------------------------------------------
-// Values pass: s0[t][pix] (direct trace A) and, for cross-correlation,
-// s0b[t][pix] (displaced trace B).
-// ---------------------------------------------------------------------------
-__global__ void c2_values_kernel(Job j, const void *stack, const float *bparams, const float *basis,
-                                 float *s0a, float *s0b)
-{
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= j.npix) return;
-    const int t0 = blockIdx.y * kVFrames, t1 = min(t0 + kVFrames, j.num);
-    for (int tr = 0; tr < (j.is_ccf ? 2 : 1); tr++) {
-        const int trace = tr ? j.npix + pix : pix;
-        int x0, y0;
-        trace_origin(j, trace, x0, y0);
-        float bp[kBleachStride];
-#pragma unroll
-        for (int i = 0; i < kBleachStride; i++) bp[i] = __ldg(&bparams[(size_t)trace * kBleachStride + i]);
-        const bool corr = j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f;
-        float *dst = tr ? s0b : s0a;
-        for (int t = t0; t < t1; t += 8) {
-            float v[8];
-            window_values<8>(j, stack, x0, y0, t, t1, v);
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int tt = t + u;
-                if (tt >= t1) break;
-                float x = v[u];
-                if (corr) {
-                    const float ft = frame_time(j, tt);
-                    x = bleach_correct(x, bleach_f(bp, j.bleach, j.poly_order, ft,
-                                                   basis ? basis + (size_t)tt * (j.poly_order + 1) : nullptr),
-                                       bp[9], bp[10]);
-                }
-                dst[(size_t)tt * j.npix + pix] = x - bp[12];
-            }
-        }
-    }
+    c.sst = c.stats + pix;
+    c.sst_stride = a.npix;
+    c.smon = nullptr;
+    c.smon_stride = 0;
+    c.lag0 = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -174,9 +163,23 @@ __device__ __forceinline__ float c2_load(const float *in, int n, int nk, int npi
     return n < nk ? __ldg(&in[(size_t)n * npix + pix]) : 0.f;
 }
 
-template <bool CCF, bool FIRST17, bool TWO, int QP>
+// Sample source of a pair kernel: level-k samples of the direct (a) and
+// delayed (b) traces from the materialised FP32 streams.  prep(g) precedes
+// the reads of group g's 16 samples (in order, jj = 0..15); acquire/release
+// bracket the groups (hooks for a source that stages its data).
+struct GlobalSrc {
+    const float *inA, *inB;
+    int nk, npix, pix;
+    __device__ __forceinline__ void prep(int) {}
+    __device__ __forceinline__ float a(int n, int) { return c2_load(inA, n, nk, npix, pix); }
+    __device__ __forceinline__ float b(int n, int) { return c2_load(inB, n, nk, npix, pix); }
+    __device__ __forceinline__ bool acquire(int) { return true; }
+    __device__ __forceinline__ void release(int) {}
+};
+
+template <bool CCF, bool FIRST17, bool TWO, int QP, class Src>
 __device__ __forceinline__ void c2_pair_group(const C2Ctx &c, const PairGeo &p, float *heads, int nt,
-                                              PairReg<FIRST17> &R, int g)
+                                              PairReg<FIRST17> &R, int g, Src &src)
 {
     constexpr int NF = PairReg<FIRST17>::NF, DF = PairReg<FIRST17>::DF;
     constexpr int PH0 = 16 * (QP & 1);
@@ -184,16 +187,17 @@ __device__ __forceinline__ void c2_pair_group(const C2Ctx &c, const PairGeo &p, 
     const int n0 = 16 * g;
     const bool dirF = (n0 - 16 >= p.sk0) && (n0 - 16 < p.sk1);          // direct samples n0-16 .. n0-1
     const bool dirS = TWO && (n0 - 32 >= p.sk0) && (n0 - 32 < p.sk1);   // second-level 8g-16 .. 8g-9
+    src.prep(g + 1);
 #pragma unroll
     for (int jj = 0; jj < 16; jj++) {
         const int n = n0 + jj;
         const float vB = R.curB[jj];
-        R.curB[jj] = c2_load(p.inB, n + 16, p.nk, c.npix, c.pix);
         R.wB[(PH0 + jj) & 31] = vB;
         if (CCF) {
             R.wA[(PH0 + jj) & 31] = R.curA[jj];
-            R.curA[jj] = c2_load(p.inA, n + 16, p.nk, c.npix, c.pix);
+            R.curA[jj] = src.a(n + 16, jj);
         }
+        R.curB[jj] = src.b(n + 16, jj);
         if (dirF) {
             // direct sample y = n - 16 with delayed samples y + DF .. y + 16 = n
             const float x0 = CCF ? R.wA[(PH0 + 16 + jj) & 31] : R.wB[(PH0 + 16 + jj) & 31];
@@ -221,7 +225,7 @@ __device__ __forceinline__ void c2_pair_group(const C2Ctx &c, const PairGeo &p, 
         }
     }
     // level-(k+2) samples 4g .. 4g+3 from second-level samples 8g .. 8g+7
-    if (TWO && p.outB) {
+    if (TWO && p.outB && c.valid) {
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int m2 = 4 * g + i;
@@ -298,20 +302,24 @@ __device__ __forceinline__ void c2_pair_group(const C2Ctx &c, const PairGeo &p, 
     }
 }
 
-template <bool CCF, bool FIRST17, bool TWO>
-__global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const float *inA, const float *inB,
-                                                             float *outA, float *outB, int k)
+// First lag of levels (k, k+1) handled by one pair pass.
+__host__ __device__ __forceinline__ int pair_lag0(int k, bool first17) { return first17 ? 0 : (kP + 1) + (k - 1) * 8; }
+
+// One (pixel, segment) of levels k and k+1: the register-ring pass over the
+// segment's level-k samples from `src`.  heads: this thread's heads (stride
+// nt floats); sst / smon (optional): shared-memory block statistics (written
+// back by the caller) and monitors of the pass's lags, from pair_lag0 on,
+// stride nt.
+template <bool CCF, bool FIRST17, bool TWO, class Src>
+__device__ __forceinline__ void c2_pair_body(const C2Args &a, Src &src, float *outA, float *outB, int k, int pix,
+                                             int seg, float *heads, int nt, float *sst = nullptr,
+                                             const float2 *smon = nullptr)
 {
-    __shared__ float heads_sm[kHeadFields * kC2Threads];
-    const int nt = blockDim.x, tid = threadIdx.x;
-    const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
-    if (pix >= a.npix) return;          // no block-wide synchronisation below
-    float *heads = heads_sm + tid;
     C2Ctx c;
     c2_ctx(c, a, pix, seg, k);
+    if (sst) { c.sst = sst; c.sst_stride = nt; c.lag0 = pair_lag0(k, FIRST17); }
+    if (smon) { c.smon = smon; c.smon_stride = nt; c.lag0 = pair_lag0(k, FIRST17); }
     PairGeo p;
-    p.inA = CCF ? inA : inB;
-    p.inB = inB;
     p.outA = outA;
     p.outB = outB;
     p.k = k;
@@ -320,7 +328,6 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
     p.nk2 = (TWO && k + 2 < a.q) ? a.numbin[k + 2] : 0;
     const int s0 = seg << a.seg_log[k];
     const int s1 = s0 + (1 << a.seg_log[k]);
-    if (s0 >= a.num) return;
     p.sk0 = s0 >> k;
     p.sk1 = s1 >= a.num ? p.nk : (s1 >> k);
     p.LF = 1 << (c.ind - k);
@@ -328,11 +335,13 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
     p.lagF = FIRST17 ? 0 : (kP + 1) + (k - 1) * 8;
     p.lagS = (kP + 1) + k * 8;
 
-    for (int lag = p.lagF; lag < p.lagF + PairReg<FIRST17>::NF; lag++)
-        for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
-    if (TWO)
-        for (int lag = p.lagS; lag < p.lagS + 8; lag++)
-            for (int st = 0; st < kStatN; st++) stat_ref(c.stats, c.npix, lag, st, pix) = 0.f;
+    if (c.valid) {
+        for (int lag = p.lagF; lag < p.lagF + PairReg<FIRST17>::NF; lag++)
+            for (int st = 0; st < kStatN; st++) c.stat(lag, st) = 0.f;
+        if (TWO)
+            for (int lag = p.lagS; lag < p.lagS + 8; lag++)
+                for (int st = 0; st < kStatN; st++) c.stat(lag, st) = 0.f;
+    }
     for (int f = 0; f < kHeadFields; f++) heads[f * nt] = 0.f;
 
     PairReg<FIRST17> R;
@@ -343,21 +352,33 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
 #pragma unroll
     for (int l = 0; l < 8; l++) R.accS[l] = 0.f;
     R.bF0 = R.bF1 = R.bS0 = R.bS1 = 0.f;
+    if (!src.acquire(0)) return;
+    src.prep(p.sk0 / 16);
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-        R.curB[i] = c2_load(p.inB, p.sk0 + i, p.nk, c.npix, pix);
-        R.curA[i] = CCF ? c2_load(p.inA, p.sk0 + i, p.nk, c.npix, pix) : 0.f;
+        R.curA[i] = CCF ? src.a(p.sk0 + i, i) : 0.f;
+        R.curB[i] = src.b(p.sk0 + i, i);
     }
     // groups of 16 samples: the segment's, then 48 more (the second level's
-    // last direct samples need 16 second-level samples past the segment)
+    // last direct samples need 16 second-level samples past the segment);
+    // group r (relative) reads the samples of group r + 1
     const int g0 = p.sk0 / 16;
     int ng = (p.sk1 - p.sk0 + 48 + 15) / 16;
     ng = (ng + 3) & ~3;
-    for (int g = g0; g < g0 + ng; g += 4) {
-        c2_pair_group<CCF, FIRST17, TWO, 0>(c, p, heads, nt, R, g);
-        c2_pair_group<CCF, FIRST17, TWO, 1>(c, p, heads, nt, R, g + 1);
-        c2_pair_group<CCF, FIRST17, TWO, 2>(c, p, heads, nt, R, g + 2);
-        c2_pair_group<CCF, FIRST17, TWO, 3>(c, p, heads, nt, R, g + 3);
+    for (int r = 0; r < ng; r += 4) {
+        const int g = g0 + r;
+        if (!src.acquire(r + 1)) return;
+        c2_pair_group<CCF, FIRST17, TWO, 0>(c, p, heads, nt, R, g, src);
+        src.release(r);
+        if (!src.acquire(r + 2)) return;
+        c2_pair_group<CCF, FIRST17, TWO, 1>(c, p, heads, nt, R, g + 1, src);
+        src.release(r + 1);
+        if (!src.acquire(r + 3)) return;
+        c2_pair_group<CCF, FIRST17, TWO, 2>(c, p, heads, nt, R, g + 2, src);
+        src.release(r + 2);
+        if (!src.acquire(r + 4)) return;
+        c2_pair_group<CCF, FIRST17, TWO, 3>(c, p, heads, nt, R, g + 3, src);
+        src.release(r + 3);
     }
     // the partial blocks at the end into the totals
 #pragma unroll
@@ -365,6 +386,36 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
     if (TWO)
 #pragma unroll
         for (int l = 0; l < 8; l++) c2_add_total(c, p.lagS + l, R.accS[l]);
+}
+
+template <bool CCF, bool FIRST17, bool TWO>
+__global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const float *inA, const float *inB,
+                                                             float *outA, float *outB, int k)
+{
+    constexpr int NL = (FIRST17 ? kP + 1 : 8) + (TWO ? 8 : 0);
+    __shared__ float heads_sm[kHeadFields * kC2Threads];
+    // block statistics and monitors of this pass's lags in shared memory: the
+    // read-modify-writes at block ends stay on chip; written back at the end
+    __shared__ float sst[NL * kStatN * kC2Threads];
+    __shared__ float2 smon[NL * kC2Threads];
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
+    if (pix >= a.npix) return;          // no block-wide synchronisation below
+    if ((seg << a.seg_log[k]) >= a.num) return;
+    const int lag0 = pair_lag0(k, FIRST17);
+    {
+        const float4 *m = a.mon + (size_t)pix * a.chanum + lag0;
+        for (int l = 0; l < NL; l++) {
+            const float4 v = __ldg(&m[l]);
+            smon[l * nt + tid] = make_float2(v.x, v.y);
+        }
+    }
+    GlobalSrc src{CCF ? inA : inB, inB, a.numbin[k], a.npix, pix};
+    c2_pair_body<CCF, FIRST17, TWO>(a, src, outA, outB, k, pix, seg, heads_sm + tid, nt, sst + tid, smon + tid);
+    float *gst = a.o.stats + (size_t)seg * a.stat_stride;
+    for (int l = 0; l < NL; l++)
+        for (int st = 0; st < kStatN; st++)
+            stat_ref(gst, a.npix, lag0 + l, st, pix) = sst[(size_t)(l * kStatN + st) * nt + tid];
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +663,7 @@ int corr_kernel_count(const Job &j)
 {
     if (!corr2_supported(j)) return 1;
     const Plan2 p = plan2(j);
-    return 1 + p.npair + (p.k_tail < j.q ? 1 : 0) + 1;
+    return p.npair + (p.k_tail < j.q ? 1 : 0) + 1;   // pair kernels, tail, finalise
 }
 
 size_t corr_stats_floats(const Job &j)
@@ -621,17 +672,20 @@ size_t corr_stats_floats(const Job &j)
     return corr2_supported(j) ? one * corr2_nseg(j) : one;
 }
 
-// Sample streams: s0 (num x npix), s2 (num/4 x npix), s4 (num/16 x npix), per trace.
+// Binned sample streams, per trace: s2 (num/4 x npix) and s4 (num/16 x
+// npix), written by the pair kernels for the next level pair.
 size_t corr_stream_floats(const Job &j)
 {
     if (!corr2_supported(j)) return 1;
     const size_t tr = j.is_ccf ? 2 : 1;
-    return tr * (size_t)j.npix * ((size_t)j.num + (size_t)(j.num >> 2) + (size_t)(j.num >> 4) + 3);
+    return tr * (size_t)j.npix * ((size_t)(j.num >> 2) + (size_t)(j.num >> 4) + 3);
 }
 
-cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
-                         const float *basis, const float4 *mon, const int *blk_ind, const CorrOut &o,
-                         float *streams, cudaStream_t stream)
+// The corrected level-0 stream s0[trace][frame][pixel] (imfcs_stream.cu).
+size_t level0_stream_floats(const Job &j) { return (size_t)(j.is_ccf ? 2 : 1) * j.npix * j.num; }
+
+cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
+                         const CorrOut &o, float *streams, cudaStream_t stream)
 {
     const Plan2 pl = plan2(j);
     C2Args a;
@@ -653,14 +707,10 @@ cudaError_t launch_corr2(const Job &j, const LagInfo *li, const void *stack, con
 
     const size_t tr = j.is_ccf ? 2 : 1;
     const size_t np = j.npix;
-    float *s0a = streams, *s0b = j.is_ccf ? s0a + np * j.num : s0a;
-    float *s2a = streams + tr * np * j.num, *s2b = j.is_ccf ? s2a + np * (j.num >> 2) : s2a;
+    const float *s0a = s0, *s0b = j.is_ccf ? s0 + np * j.num : s0;
+    float *s2a = streams, *s2b = j.is_ccf ? s2a + np * (j.num >> 2) : s2a;
     float *s4a = s2a + tr * np * (j.num >> 2), *s4b = j.is_ccf ? s4a + np * (j.num >> 4) : s4a;
-
-    dim3 vgrid((j.npix + 127) / 128, (j.num + kVFrames - 1) / kVFrames);
-    c2_values_kernel<<<vgrid, 128, 0, stream>>>(j, stack, bparams, basis, s0a, s0b);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
 
     const int pgx = (j.npix + kC2Threads - 1) / kC2Threads;
     for (int i = 0; i < pl.npair; i++) {

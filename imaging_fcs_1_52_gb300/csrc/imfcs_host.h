@@ -10,13 +10,14 @@ namespace imfcs {
 
 // launchers (defined in the kernel translation units)
 cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, const float *bparams,
-                        const float *basis, const float4 *mon, const int *blk_ind, double *acf,
+                        const float *basis, const float *s0, const float4 *mon, const int *blk_ind, double *acf,
                         double *var, double *sd, double *nb_mean, double *nb_cov, float *bprod,
                         int pnum_stride, float *stats, float *streams, int gls, int *err,
                         cudaStream_t stream);
 size_t corr_smem_bytes(int q, bool ccf);
 size_t corr_stats_floats(const Job &j);    // per-lag block statistics scratch (floats)
-size_t corr_stream_floats(const Job &j);   // sample streams of the correlator chain (floats)
+size_t corr_stream_floats(const Job &j);   // binned sample streams of the correlator chain (floats)
+size_t level0_stream_floats(const Job &j); // the corrected level-0 stream s0 (floats)
 int corr_kernel_count(const Job &j);        // kernels one correlator launch issues
 
 struct FitArgs;
@@ -35,13 +36,14 @@ cudaError_t launch_trace(const Job &j, const void *stack, float *trace, cudaStre
 cudaError_t launch_bleach(const Job &j, const float *trace, const double *proj, float uscale,
                           float uoff, float *bparams, cudaStream_t s);
 cudaError_t launch_center_given(const Job &j, const float *trace, float *bparams, cudaStream_t s);
-cudaError_t launch_monitor(const Job &j, const LagInfo *li_dev, const void *stack,
-                           const float *bparams, const float *basis, const int *snap_pos, int nseg,
-                           float2 *segtot, float2 *snap_part, float4 *mon, float4 *blkmon,
-                           cudaStream_t s);
-cudaError_t launch_block(const Job &j, const void *stack, const float *bparams, const float *basis,
-                         const float4 *blkmon, int nbseg, float *s1, float *s2, float *segsum,
-                         int *ind, int *ok, cudaStream_t s);
+cudaError_t launch_stream(const Job &j, const void *stack, const float *bparams, const float *basis,
+                          const int *snap_pos, int nseg, float *s0, float2 *segtot, float2 *snap_part, int *segbad,
+                          int *snap_bad, int *err, cudaStream_t s);
+cudaError_t launch_monitor_finalize(const Job &j, const LagInfo *li_dev, const float *bparams, int nseg,
+                                    const float2 *segtot, const float2 *snap_part, const int *segbad,
+                                    const int *snap_bad, float4 *mon, float4 *blkmon, cudaStream_t s);
+cudaError_t launch_block(const Job &j, const float *s0, const float4 *blkmon, int nbseg, float *s1, float *s2,
+                         float *segsum, int *ind, int *ok, cudaStream_t s);
 cudaError_t launch_binning(const float *in, float *out, int win, int hin, int wt, int ht,
                            int frames, int bx, int by, cudaStream_t s);
 cudaError_t launch_bleach_average(const float *in, float *out, int w, int h, int nopit, int ave,

@@ -217,12 +217,13 @@ __device__ __forceinline__ float bleach_f(const float *bp, int mode, int order, 
     }
 }
 
-// v / sqrt(f/f0) + f0 (1 - sqrt(f/f0)) with one reciprocal square root.
+// v / sqrt(f/f0) + f0 (1 - sqrt(f/f0)) with one reciprocal square root,
+// written as (v - f) / sqrt(f/f0) + f0 (f0 sqrt(f/f0) = f / sqrt(f/f0)):
+// one subtraction, one FMA, and no 1 - sqrt(f/f0) cancellation when the
+// curve is near f0.
 __device__ __forceinline__ float bleach_correct(float v, float f, float f0, float inv_f0)
 {
-    float r = f * inv_f0;
-    float rs = rsqrtf(r);
-    return fmaf(v, rs, f0 * (1.f - r * rs));
+    return fmaf(v - f, rsqrtf(f * inv_f0), f0);
 }
 
 // Time of frame t (0-based) in the correction: frametime * (x + 0.5) with the

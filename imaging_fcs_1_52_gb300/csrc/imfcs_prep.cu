@@ -1,11 +1,12 @@
 // imfcs_prep.cu -- the passes in front of the correlator:
 //   trace_kernel       averaged intensity trace (calcIntensityTrace, java:9822-9855)
 //   bleach_*_kernel    polynomial / exponential bleach fits (java:10845-11004)
-//   monitor_kernel     prefix sums of the corrected, centred trace at the
-//                      window edges every lag's monitors need (java:9484-9491)
-//   block_kernel       lag-1 blocking curve of blockTransform (java:9217-9422)
-// All streaming passes read the stack once and are HBM-bound; they split the
-// time axis into segments so that every SM has enough loads in flight.
+//   monitor_finalize_kernel  the lags' monitors from the partial sums the
+//                      streaming pass (imfcs_stream.cu) wrote (java:9484-9491)
+//   block_kernel       lag-1 blocking curve of blockTransform (java:9217-9422),
+//                      from the corrected level-0 stream
+// The streaming passes split the time axis into segments so that every SM
+// has enough loads in flight.
 #include <math.h>
 
 #include "imfcs_internal.cuh"
@@ -77,23 +78,27 @@ __global__ void bleach_poly_kernel(Job j, const float *trace, const double *proj
     double f0 = 0.0;
     for (int i = 0; i < k; i++) f0 += c[i] * (double)lb[i];
     float f0f = (float)f0, inv_f0 = (float)(1.0 / f0);
-    // centre: mean of the corrected averaged trace
-    float csum = 0.f;
+    // centre: mean of the finite points of the corrected averaged trace (a
+    // shift the correlator removes exactly; non-finite points, where the
+    // curve crosses zero, are left out so that they cannot spread)
+    float csum = 0.f, cnt = 0.f;
     for (int x = lane; x < j.nopit; x += 32) {
         float t = j.frametime * ((float)x + 0.5f) * (float)j.ave;
         legendre(t * uscale + uoff, j.poly_order, lb);
         float f = 0.f;
         for (int i = 0; i < k; i++) f = fmaf(cf[i], lb[i], f);
-        csum += bleach_correct(__ldg(&y[x]), f, f0f, inv_f0);
+        const float v = bleach_correct(__ldg(&y[x]), f, f0f, inv_f0);
+        if (isfinite(v)) { csum += v; cnt += 1.f; }
     }
     csum = warp_sum(csum);
+    cnt = warp_sum(cnt);
     if (lane == 0) {
         float *bp = bp_out + (size_t)tr * kBleachStride;
         for (int i = 0; i < k; i++) bp[i] = cf[i];
         bp[9] = f0f;
         bp[10] = inv_f0;
         bp[11] = (isfinite(f0) && f0 != 0.0) ? 1.f : 0.f;
-        bp[12] = csum / j.nopit;
+        bp[12] = cnt > 0.f ? csum / cnt : 0.f;
         bp[13] = uscale;
         bp[14] = uoff;
     }
@@ -125,22 +130,24 @@ __global__ void center_kernel(Job j, const float *trace, float *bp_out)
 //     f0 = f(0),  s_c = A_c / tau_c,  k_c = 1 / tau_c >= 0,
 //     f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c,
 // which stay well conditioned when a component is slow (k_c t << 1, where
-// the reference's A and C grow without bound while A + C stays finite).
+// the reference's A and C grow without bound while A + C stays finite) and
+// are continuous through k_c = 0 (tau = infinity), so a trace whose minimum
+// lies at or beyond that valley (k_c <= 0, a non-decaying trace) reaches it.
 // Scaled variables t / tmax, y / ymax; one warp per trace.
-//   phase 1: FP32 model and normal equations until the Gauss-Newton step is
-//            below 1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
-//   phase 2: model values and residuals in float-float (the exponentials by
-//            a per-lane recurrence), Jacobian and normal equations in FP32,
-//            until the step is below 1e-5 sigma + 1e-7 |p|.
-// A rate at its bound k = 0 whose Gauss-Newton step points below it is held
-// fixed (active set).
+//   phase 1: FP32 Levenberg-Marquardt until the Gauss-Newton step is below
+//            1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
+//   phase 2: Newton with the full Hessian of chi^2/2 (J^T J - sum r d2f; the
+//            Gauss-Newton matrix alone does not contract on these
+//            large-residual problems), residuals and gradient in float-float
+//            (the exponentials by a per-lane recurrence), to the least-squares
+//            minimum: until the step is below 1e-9 sigma + 1e-12 |p|.
 // ---------------------------------------------------------------------------
 
 // u = (1 - e^{-kt}) / k and du/dk in FP32, x = k t >= 0 (ik = 1/k).
 __device__ __forceinline__ void exp_u_f(float k, float ik, float t, float &u, float &dudk)
 {
     const float x = k * t;
-    if (x < 0.05f) {
+    if (fabsf(x) < 0.05f) {
         u = slow_exp_term(k, t);
         // du/dk = -t^2 (1/2 - x/3 + x^2/8 - x^3/30 + x^4/144)
         float d = fmaf(x, 1.f / 144.f, -1.f / 30.f);
@@ -159,7 +166,7 @@ __device__ __forceinline__ void exp_u_f(float k, float ik, float t, float &u, fl
 __device__ __forceinline__ float exp_dudk(float k, float ik, float t, float e, float u)
 {
     const float x = k * t;
-    if (x < 0.05f) {
+    if (fabsf(x) < 0.05f) {
         float d = fmaf(x, 1.f / 144.f, -1.f / 30.f);
         d = fmaf(x, d, 1.f / 8.f);
         d = fmaf(x, d, -1.f / 3.f);
@@ -244,18 +251,38 @@ __device__ bool solve_scaled_k(const float *A, const float *b, float lambda, uns
     return true;
 }
 
-// chi^2 and the normal equations A = J^T J, g = J^T r of the scaled model at
-// p over the trace (warp).  precise: model values and residuals in
-// float-float (the exponentials by a per-lane recurrence e <- e q seeded in
-// FP64), chi^2 summed in float-float; otherwise FP32.
+// d2u/dk2 of u = (1 - e^{-kt}) / k from e = e^{-kt} and u_k (series for
+// small |x|, x = kt: t^3 (1/3 - x/4 + x^2/10 - x^3/36 + x^4/168)).
+__device__ __forceinline__ float exp_d2udk2(float k, float ik, float t, float e, float uk)
+{
+    const float x = k * t;
+    if (fabsf(x) < 0.05f) {
+        float d = fmaf(x, 1.f / 168.f, -1.f / 36.f);
+        d = fmaf(x, d, 0.1f);
+        d = fmaf(x, d, -0.25f);
+        d = fmaf(x, d, 1.f / 3.f);
+        return t * t * t * d;
+    }
+    return (-t * t * e - 2.f * uk) * ik;
+}
+
+// One evaluation of the scaled model at p over the trace (warp).
+//   precise = false: FP32 residuals, A = J^T J (Gauss-Newton matrix), g = J^T r;
+//   precise = true:  residuals in float-float (the exponentials by a per-lane
+//                    recurrence e <- e q seeded in FP64), A = the full Hessian
+//                    of chi^2/2, J^T J - sum_i r_i d2f_i (FP32), g = J^T r
+//                    accumulated in float-float and reduced in FP64.
+// Returns chi^2 (float-float summed when precise).
 template <int K>
 __device__ __noinline__ double exp_normal(const float *y, int n, float dts, float iy, const double *p, bool precise,
-                             float *A, float *g, int lane)
+                                          float *A, double *g, int lane)
 {
     constexpr int NC = (K - 1) / 2;
-    constexpr int NA = K * (K + 1) / 2 + K;
-    float acc[NA];
+    constexpr int NA = K * (K + 1) / 2;
+    float acc[NA], gf[K];
+    f2 gp[K];
     for (int i = 0; i < NA; i++) acc[i] = 0.f;
+    for (int i = 0; i < K; i++) { gf[i] = 0.f; gp[i] = {0.f, 0.f}; }
     float pf[K], ik[NC];
     for (int i = 0; i < K; i++) pf[i] = (float)p[i];
     for (int c = 0; c < NC; c++) ik[c] = 1.f / pf[2 + 2 * c];
@@ -267,17 +294,17 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
             const double k = p[2 + 2 * c];
             e[c] = f2_from_d(exp(-k * ((double)lane + 0.5) * (double)dts));
             q[c] = f2_from_d(exp(-k * 32.0 * (double)dts));
-            slow[c] = k * (double)n * (double)dts < 1e-4;
+            slow[c] = fabs(k * (double)n * (double)dts) < 1e-4;
             invk[c] = f2_from_d(slow[c] ? 0.0 : 1.0 / k);
             sp[c] = f2_from_d(p[1 + 2 * c]);
         }
     }
-    double c2d = 0.0;
     float c2f = 0.f;            // FP32 phase: per-lane sum of ~n/32 squares
     f2 c2 = {0.f, 0.f};
     for (int x = lane; x < n; x += 32) {
         const float t = ((float)x + 0.5f) * dts;
         float gr[K], r;
+        float hsk[NC], hkk[NC];   // d2f/(ds dk), d2f/dk2 per component (precise)
         gr[0] = 1.f;
         if (!precise) {
             float f = pf[0];
@@ -296,7 +323,7 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
             for (int c = 0; c < NC; c++) {
                 f2 u;
                 if (slow[c]) {
-                    // u = t (1 - corr), corr = x/2 - x^2/6 + x^3/24 (x < 1e-4)
+                    // u = t (1 - corr), corr = x/2 - x^2/6 + x^3/24 (|x| < 1e-4)
                     const float xx = pf[2 + 2 * c] * t;
                     const float corr = xx * (0.5f - xx * (1.f / 6.f - xx * (1.f / 24.f)));
                     u = f2_add(tf, f2_neg(f2_two_prod(tf.hi, corr)));
@@ -304,19 +331,33 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
                     u = f2_mul(f2_add({1.f, 0.f}, f2_neg(e[c])), invk[c]);
                 }
                 f = f2_add(f, f2_neg(f2_mul(sp[c], u)));
-                const float uf = u.hi + u.lo;
+                const float uf = u.hi + u.lo, ef = e[c].hi + e[c].lo;
+                const float uk = exp_dudk(pf[2 + 2 * c], ik[c], t, ef, uf);
                 gr[1 + 2 * c] = -uf;
-                gr[2 + 2 * c] = -pf[1 + 2 * c] * exp_dudk(pf[2 + 2 * c], ik[c], t, e[c].hi + e[c].lo, uf);
+                gr[2 + 2 * c] = -pf[1 + 2 * c] * uk;
+                hsk[c] = -uk;
+                hkk[c] = -pf[1 + 2 * c] * exp_d2udk2(pf[2 + 2 * c], ik[c], t, ef, uk);
                 e[c] = f2_mul(e[c], q[c]);
             }
             const f2 rr = f2_add(f2_two_prod(__ldg(&y[x]), iy), f2_neg(f));
             r = rr.hi + rr.lo;
             c2 = f2_add(c2, f2_mul(rr, rr));
+            for (int a = 0; a < K; a++) gp[a] = f2_add(gp[a], f2_two_prod(gr[a], rr.hi));
+            for (int a = 0; a < K; a++) gp[a] = f2_add(gp[a], f2_two_prod(gr[a], rr.lo));
         }
         int qa = 0;
         for (int a = 0; a < K; a++)
             for (int b = 0; b <= a; b++) acc[qa++] += gr[a] * gr[b];
-        for (int a = 0; a < K; a++) acc[qa++] += gr[a] * r;
+        if (precise) {
+            // - r d2f: the only nonzero second derivatives are (s_c, k_c) and (k_c, k_c)
+            for (int c = 0; c < NC; c++) {
+                const int is = 1 + 2 * c, ikk = 2 + 2 * c;
+                acc[ikk * (ikk + 1) / 2 + is] -= r * hsk[c];
+                acc[ikk * (ikk + 1) / 2 + ikk] -= r * hkk[c];
+            }
+        } else {
+            for (int a = 0; a < K; a++) gf[a] += gr[a] * r;
+        }
     }
     int qa = 0;
     for (int a = 0; a < K; a++)
@@ -325,23 +366,21 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
             A[a * K + b] = v;
             A[b * K + a] = v;
         }
-    for (int a = 0; a < K; a++) g[a] = warp_sum(acc[qa++]);
-    c2d = precise ? (double)c2.hi + (double)c2.lo : (double)c2f;
+    for (int a = 0; a < K; a++)
+        g[a] = precise ? warp_sum_d((double)gp[a].hi + (double)gp[a].lo) : (double)warp_sum(gf[a]);
+    const double c2d = precise ? (double)c2.hi + (double)c2.lo : (double)c2f;
     return warp_sum_d(c2d);
 }
 
-// Held rates (bit mask) and the undamped Gauss-Newton step.
+// The undamped (Gauss-)Newton step on A h = g.  Rates k may take either
+// sign: the rate form is continuous through k = 0 (tau = infinity), so a
+// non-decaying trace reaches its minimum (k <= 0) instead of a bound.
 template <int K>
-__device__ __forceinline__ bool exp_gn_step(const float *A, const float *g, const double *p, unsigned &fix,
-                                            float *h)
+__device__ __forceinline__ bool exp_newton_step(const float *A, const double *gd, float *h)
 {
-    constexpr int NC = (K - 1) / 2;
-    fix = 0;
-    bool ok = solve_scaled_k<K>(A, g, 0.f, 0u, h);
-    for (int c = 0; c < NC; c++)
-        if (p[2 + 2 * c] <= 0.0 && (!ok || h[2 + 2 * c] < 0.f)) fix |= 1u << (2 + 2 * c);
-    if (fix) ok = solve_scaled_k<K>(A, g, 0.f, fix, h);
-    return ok;
+    float g[K];
+    for (int a = 0; a < K; a++) g[a] = (float)gd[a];
+    return solve_scaled_k<K>(A, g, 0.f, 0u, h);
 }
 
 template <int K>
@@ -373,57 +412,72 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
             p[0] = y1; p[1] = 0.5 * y1 / t10; p[2] = 1.0 / t10; p[3] = 0.5 * y1 / thalf; p[4] = 1.0 / thalf;
         }
     }
-    float A[K * K], g[K], lambda = 1e-3f;
-    bool precise = false;
-    double chi2 = exp_normal<K>(y, n, dts, iy, p, precise, A, g, lane);
+    // Phase 1: FP32 Levenberg-Marquardt until the Gauss-Newton step is below
+    // 1e-4 sigma + 1e-6 |p| (or no step lowers chi^2 up to lambda 1e10).
+    float A[K * K], lambda = 1e-3f;
+    double g[K];
+    double chi2 = exp_normal<K>(y, n, dts, iy, p, false, A, g, lane);
     const bool ok = isfinite(chi2);
-    int nprec = 0;
+    int evals = 1;
     for (int it_n = 0; ok && it_n < 400; it_n++) {
-        unsigned fix;
         float h[K];
-        if (exp_gn_step<K>(A, g, p, fix, h)) {
+        if (exp_newton_step<K>(A, g, h)) {
             bool conv = true;
             for (int a = 0; a < K; a++) {
-                if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
-                conv = conv && fabsf(h[a]) <= (precise ? 1e-7f : 1e-6f) * (float)fabs(p[a]) +
-                                                  (precise ? 1e-5f : 1e-4f) * sig;
+                conv = conv && fabsf(h[a]) <= 1e-6f * (float)fabs(p[a]) + 1e-4f * sig;
             }
-            if (conv) {
-                if (precise) break;
-                precise = true;
-                chi2 = exp_normal<K>(y, n, dts, iy, p, true, A, g, lane);
-                lambda = 1e-3f;
-                continue;
-            }
+            if (conv) break;
         }
-        bool stalled = false;
-        if (!solve_scaled_k<K>(A, g, lambda, fix, h)) {
+        float gf[K];
+        for (int a = 0; a < K; a++) gf[a] = (float)g[a];
+        if (!solve_scaled_k<K>(A, gf, lambda, 0u, h)) {
             lambda *= 10.f;
-            stalled = lambda > 1e10f;
+            if (lambda > 1e10f) break;
+            continue;
+        }
+        double pn[K];
+        for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
+        float An[K * K];
+        double gn[K];
+        const double c2n = exp_normal<K>(y, n, dts, iy, pn, false, An, gn, lane);
+        evals++;
+        if (isfinite(c2n) && c2n < chi2) {
+            for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
+            for (int a = 0; a < K * K; a++) A[a] = An[a];
+            chi2 = c2n;
+            lambda = fmaxf(lambda * 0.1f, 1e-12f);
         } else {
+            lambda *= 10.f;
+            if (lambda > 1e10f) break;
+        }
+    }
+    // Phase 2: Newton with the full Hessian, float-float residuals and
+    // gradient, to the least-squares minimum: until the step is below
+    // 1e-9 sigma + 1e-12 |p|, while chi^2 does not increase.
+    if (ok) {
+        chi2 = exp_normal<K>(y, n, dts, iy, p, true, A, g, lane);
+        evals++;
+        for (int it_n = 0; it_n < 20 && isfinite(chi2); it_n++) {
+            float h[K];
+            if (!exp_newton_step<K>(A, g, h)) break;   // Hessian not positive definite
+            bool conv = true;
+            for (int a = 0; a < K; a++) {
+                const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
+                conv = conv && fabsf(h[a]) <= 1e-12f * (float)fabs(p[a]) + 1e-9f * sig;
+            }
             double pn[K];
             for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
-            for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
-            float An[K * K], gn[K];
-            const double c2n = exp_normal<K>(y, n, dts, iy, pn, precise, An, gn, lane);
-            if (isfinite(c2n) && c2n < chi2) {
-                for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
-                for (int a = 0; a < K * K; a++) A[a] = An[a];
-                chi2 = c2n;
-                lambda = fmaxf(lambda * 0.1f, 1e-12f);
-            } else {
-                lambda *= 10.f;
-                stalled = lambda > 1e10f;
-            }
+            float An[K * K];
+            double gn[K];
+            const double c2n = exp_normal<K>(y, n, dts, iy, pn, true, An, gn, lane);
+            evals++;
+            if (!(isfinite(c2n) && c2n <= chi2)) break;
+            for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
+            for (int a = 0; a < K * K; a++) A[a] = An[a];
+            chi2 = c2n;
+            if (conv) break;
         }
-        if (stalled) {
-            if (precise) break;
-            precise = true;
-            chi2 = exp_normal<K>(y, n, dts, iy, p, true, A, g, lane);
-            lambda = 1e-3f;
-        }
-        if (precise && ++nprec > 60) break;
     }
     // back to data units: y = y_s / iy, t = t_s tmax
     const double st = (double)dts / dt_pt;            // 1 / tmax
@@ -444,7 +498,7 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     for (int c = 0; c < NC; c++) {
         const double amp = sd[c] / kd[c];               // A_c (inf when k_c = 0)
         bpl[5 + c] = (float)kd[c];
-        if (kd[c] * t_end <= 0.5) {
+        if (fabs(kd[c]) * t_end <= 0.5) {
             flags |= 1 << c;
             bpl[7 + c] = (float)sd[c];
         } else {
@@ -460,99 +514,26 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     bpl[13] = (float)cconst;
     bpl[14] = (float)flags;
     const float f0 = (float)f0d, inv_f0 = (float)(1.0 / f0d);
-    float csum = 0.f;
+    float csum = 0.f, cnt = 0.f;     // centre over the finite corrected points
     for (int x = lane; x < n; x += 32) {
         float yx = __ldg(&y[x]);
         if (valid) {
             float t = j.frametime * ((float)x + 0.5f) * (float)j.ave;
             yx = bleach_correct(yx, bleach_f(bpl, j.bleach, 0, t, nullptr), f0, inv_f0);
         }
-        csum += yx;
+        if (isfinite(yx)) { csum += yx; cnt += 1.f; }
     }
     csum = warp_sum(csum);
+    cnt = warp_sum(cnt);
     if (lane == 0) {
         float *bp = bp_out + (size_t)tr * kBleachStride;
         for (int a = 0; a < kBleachStride; a++) bp[a] = bpl[a];
         bp[9] = f0;
         bp[10] = inv_f0;
         bp[11] = valid ? 1.f : 0.f;
-        bp[12] = csum / n;
+        bp[12] = cnt > 0.f ? csum / cnt : 0.f;
+        bp[15] = (float)evals;      // model evaluations (diagnostic)
     }
-}
-
-// ---------------------------------------------------------------------------
-// Corrected, centred frame value of a trace (the value the correlator uses).
-// basis: Legendre table [num][order+1] for the polynomial mode.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float correct_value(const Job &j, float v, int t, const float *bp,
-                                               const float *basis)
-{
-    if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
-        float tt = frame_time(j, t);
-        float f = bleach_f(bp, j.bleach, j.poly_order, tt,
-                           basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
-        v = bleach_correct(v, f, bp[9], bp[10]);
-    }
-    return v - bp[12];
-}
-
-__device__ __forceinline__ float corrected_delta(const Job &j, const void *stack, int x0, int y0,
-                                                 int t, const float *bp, const float *basis)
-{
-    float v = window_value(j, stack, x0, y0, t);
-    if (j.bleach != IMFCS_BLEACH_NONE && bp[11] != 0.f) {
-        float tt = frame_time(j, t);
-        float f = bleach_f(bp, j.bleach, j.poly_order, tt,
-                           basis ? basis + (size_t)t * (j.poly_order + 1) : nullptr);
-        v = bleach_correct(v, f, bp[9], bp[10]);
-    }
-    return v - bp[12];
-}
-
-// ---------------------------------------------------------------------------
-// Monitor pass: per (trace, segment of kSeg frames) the float-float segment
-// total of the centred trace and, for every snapshot position p inside the
-// segment, the partial sum from the segment start up to frame p-1.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) monitor_kernel(Job j, const void *stack,
-                                                      const float *bparams, const float *basis,
-                                                      const int *snap_pos, int nseg,
-                                                      float2 *segtot, float2 *snap_part)
-{
-    const int tr = blockIdx.x * blockDim.x + threadIdx.x;
-    const int seg = blockIdx.y;
-    if (tr >= j.ntrace) return;
-    int x0, y0;
-    trace_origin(j, tr, x0, y0);
-    const float *bp = bparams + (size_t)tr * kBleachStride;
-    float bpl[kBleachStride];
-    for (int i = 0; i < kBleachStride; i++) bpl[i] = __ldg(&bp[i]);
-    const int t0 = seg * kSeg, t1 = min(t0 + kSeg, j.num);
-    // first snapshot with position > t0
-    int lo = 0, hi = j.nsnap;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(&snap_pos[mid]) <= t0) lo = mid + 1; else hi = mid;
-    }
-    int sj = lo;
-    int next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
-    ff acc = {0.f, 0.f};
-    for (int tb = t0; tb < t1; tb += 8) {
-        float v[8];
-        window_values<8>(j, stack, x0, y0, tb, t1, v);
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int t = tb + u;
-            if (t >= t1) break;
-            ff_add(acc, correct_value(j, v[u], t, bpl, basis));
-            while (t + 1 == next) {
-                snap_part[(size_t)tr * j.nsnap + sj] = make_float2(acc.hi, acc.lo);
-                sj++;
-                next = sj < j.nsnap ? __ldg(&snap_pos[sj]) : 0x7fffffff;
-            }
-        }
-    }
-    segtot[(size_t)tr * nseg + seg] = make_float2(acc.hi, acc.lo);
 }
 
 // Finalise monitors: one warp per output pixel.  Exclusive scan of the
@@ -560,50 +541,68 @@ __global__ void __launch_bounds__(128) monitor_kernel(Job j, const void *stack,
 //   a = sum(direct window)/n - 2^k c0,  b = sum(delayed window)/n - 2^k c1,
 // dm = a + 2^k c0, Dm = b + 2^k c1  (java:9484-9491), plus the lag-1 monitors
 // of the zero-led sequence blockTransform reads (java:9259-9272).
+//
+// Non-finite corrected frames entered the sums as 0 and are counted; a
+// window that contains one gives a NaN monitor, so exactly the lags whose
+// windows hold a bad frame become non-finite, as calculateCF's sums do
+// (java:9484-9491).
 __global__ void monitor_finalize_kernel(Job j, const LagInfo *li, const float *bparams,
                                         int nseg, const float2 *segtot, const float2 *snap_part,
-                                        float4 *mon, float4 *blkmon)
+                                        const int *segbad, const int *snap_bad, float4 *mon, float4 *blkmon)
 {
     extern __shared__ double sh[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int pix = blockIdx.x * (blockDim.x >> 5) + wid;
     if (pix >= j.npix) return;
-    double *scan = sh + (size_t)wid * (nseg + 1 + 2 * j.nsnap);
+    double *scan = sh + (size_t)wid * (nseg + 1 + 4 * j.nsnap);
     double *pre0 = scan + nseg + 1;
     double *pre1 = pre0 + j.nsnap;
+    double *bad0 = pre1 + j.nsnap;      // prefix counts of non-finite frames
+    double *bad1 = bad0 + j.nsnap;
     for (int which = 0; which < (j.is_ccf ? 2 : 1); which++) {
         int tr = which ? j.npix + pix : pix;
         double *pre = which ? pre1 : pre0;
-        // exclusive scan of segment totals
-        double carry = 0.0;
-        for (int s0 = 0; s0 < nseg; s0 += 32) {
-            int s = s0 + lane;
-            double v = 0.0;
-            if (s < nseg) { float2 t = segtot[(size_t)tr * nseg + s]; v = (double)t.x + (double)t.y; }
-            double incl = v;
-            for (int o = 1; o < 32; o <<= 1) {
-                double u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += u;
+        double *bpre = which ? bad1 : bad0;
+        // exclusive scans of the segment totals (pass 0) and of the
+        // non-finite frame counts (pass 1), then the snapshot prefixes
+        for (int pass = 0; pass < 2; pass++) {
+            double carry = 0.0;
+            for (int s0 = 0; s0 < nseg; s0 += 32) {
+                int s = s0 + lane;
+                double v = 0.0;
+                if (s < nseg) {
+                    if (pass == 0) { float2 t = segtot[(size_t)tr * nseg + s]; v = (double)t.x + (double)t.y; }
+                    else v = (double)segbad[(size_t)tr * nseg + s];
+                }
+                double incl = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    double u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                if (s < nseg) scan[s] = carry + incl - v;
+                carry += __shfl_sync(0xffffffffu, incl, 31);
             }
-            if (s < nseg) scan[s] = carry + incl - v;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-        }
-        if (lane == 0) scan[nseg] = carry;
-        __syncwarp();
-        for (int sj = lane; sj < j.nsnap; sj += 32) {
-            int p = li->snap_pos[sj];
-            double v = 0.0;
-            if (p > 0) {
-                int seg = (p - 1) / kSeg;
-                float2 t = snap_part[(size_t)tr * j.nsnap + sj];
-                v = scan[seg] + (double)t.x + (double)t.y;
+            if (lane == 0) scan[nseg] = carry;
+            __syncwarp();
+            for (int sj = lane; sj < j.nsnap; sj += 32) {
+                int p = li->snap_pos[sj];
+                double v = 0.0;
+                if (p > 0) {
+                    int seg = (p - 1) / kSeg;
+                    if (pass == 0) {
+                        float2 t = snap_part[(size_t)tr * j.nsnap + sj];
+                        v = scan[seg] + (double)t.x + (double)t.y;
+                    } else {
+                        v = scan[seg] + (double)snap_bad[(size_t)tr * j.nsnap + sj];
+                    }
+                }
+                (pass == 0 ? pre : bpre)[sj] = v;
             }
-            pre[sj] = v;
+            __syncwarp();
         }
-        __syncwarp();
     }
     if (!j.is_ccf)
-        for (int sj = lane; sj < j.nsnap; sj += 32) pre1[sj] = pre0[sj];
+        for (int sj = lane; sj < j.nsnap; sj += 32) { pre1[sj] = pre0[sj]; bad1[sj] = bad0[sj]; }
     __syncwarp();
     const double c0 = bparams[(size_t)pix * kBleachStride + 12];
     const double c1 = bparams[(size_t)(j.is_ccf ? j.npix + pix : pix) * kBleachStride + 12];
@@ -612,6 +611,8 @@ __global__ void monitor_finalize_kernel(Job j, const LagInfo *li, const float *b
         double n = li->prodnum[x];
         double a = pre0[li->snap_dir_end[x]] / n;
         double b = (pre1[li->snap_del_end[x]] - pre1[li->snap_del_beg[x]]) / n;
+        if (bad0[li->snap_dir_end[x]] > 0.0) a = nan("");
+        if (bad1[li->snap_del_end[x]] - bad1[li->snap_del_beg[x]] > 0.0) b = nan("");
         double sc = (double)(1 << k);
         mon[(size_t)pix * j.chanum + x] =
             make_float4((float)a, (float)b, (float)(a + sc * c0), (float)(b + sc * c1));
@@ -620,6 +621,8 @@ __global__ void monitor_finalize_kernel(Job j, const LagInfo *li, const float *b
         double T1 = j.num - 1;
         double dm1 = (pre0[li->snap_tm2] + (j.num - 2) * c0) / T1;   // zero-led direct window
         double Dm1 = (pre1[li->snap_tm1] + (j.num - 1) * c1) / T1;
+        if (bad0[li->snap_tm2] > 0.0) dm1 = nan("");
+        if (bad1[li->snap_tm1] > 0.0) Dm1 = nan("");
         blkmon[pix] = make_float4((float)(dm1 - c0), (float)(Dm1 - c1), (float)dm1, (float)Dm1);
     }
 }
@@ -633,46 +636,39 @@ __global__ void monitor_finalize_kernel(Job j, const LagInfo *li, const float *b
 // and squared block means of the complete blocks inside its segment, and the
 // segment sum for the higher levels.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) block_kernel(Job j, const void *stack,
-                                                    const float *bparams, const float *basis,
-                                                    const float4 *blkmon, int nbseg,
-                                                    float *s1, float *s2, float *segsum)
+__global__ void __launch_bounds__(128) block_kernel(Job j, const float *s0a, const float *s0b,
+                                                    const float4 *blkmon, int nbseg, float *s1, float *s2,
+                                                    float *segsum)
 {
     const int pix = blockIdx.x * blockDim.x + threadIdx.x;
     const int seg = blockIdx.y;
     if (pix >= j.npix) return;
-    int xa, ya, xb, yb;
-    trace_origin(j, pix, xa, ya);
-    const int trb = j.is_ccf ? j.npix + pix : pix;
-    trace_origin(j, trb, xb, yb);
-    float bpa[kBleachStride], bpb[kBleachStride];
-    for (int i = 0; i < kBleachStride; i++) {
-        bpa[i] = __ldg(&bparams[(size_t)pix * kBleachStride + i]);
-        bpb[i] = __ldg(&bparams[(size_t)trb * kBleachStride + i]);
-    }
+    const float *sb = j.is_ccf ? s0b : s0a;
     const float4 bm = blkmon[pix];   // a1 = dm1 - c0, b1 = Dm1 - c1, dm1, Dm1
     const int nprod = j.num - 1;
     const int j0 = seg * kBlkSeg, j1 = min(j0 + kBlkSeg, nprod);
     float S1[kBlkSegLog + 1], S2[kBlkSegLog + 1], pend[kBlkSegLog + 1];
     for (int y = 0; y <= kBlkSegLog; y++) { S1[y] = 0.f; S2[y] = 0.f; pend[y] = 0.f; }
-    // direct element of product jj is J_jj = v_{jj-1} (J_0 = 0)
-    float u_prev;
-    if (j0 == 0) u_prev = -bm.z;
-    else u_prev = corrected_delta(j, stack, xa, ya, j0 - 1, bpa, basis) - bm.x;
+    // direct element of product jj is J_jj = v_{jj-1} (J_0 = 0); s0 holds the
+    // corrected values centred on c, so J - dm1 = s0 - (dm1 - c)
+    float u_prev = (j0 == 0) ? -bm.z : __ldg(&s0a[(size_t)(j0 - 1) * j.npix + pix]) - bm.x;
     float segv = 0.f;
     for (int tb = j0; tb < j1; tb += 8) {
         float va[8], vb[8];
-        window_values<8>(j, stack, xa, ya, tb, j1, va);
-        if (j.is_ccf) window_values<8>(j, stack, xb, yb, tb, j1, vb);
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const bool in = tb + u < j1;
+            va[u] = in ? __ldg(&s0a[(size_t)(tb + u) * j.npix + pix]) : 0.f;
+            vb[u] = (in && j.is_ccf) ? __ldg(&sb[(size_t)(tb + u) * j.npix + pix]) : va[u];
+        }
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const int jj = tb + u;
             if (jj >= j1) break;
-            float da = correct_value(j, va[u], jj, bpa, basis);
-            float w = (j.is_ccf ? correct_value(j, vb[u], jj, bpb, basis) : da) - bm.y;
-            float p = u_prev * w;
-            u_prev = da - bm.x;   // next direct element J_{jj+1} = v_jj
-            int rel = jj - j0;
+            const float w = vb[u] - bm.y;
+            const float p = u_prev * w;
+            u_prev = va[u] - bm.x;   // next direct element J_{jj+1} = v_jj
+            const int rel = jj - j0;
             S1[0] += p;
             S2[0] += p * p;
             float v = p;
@@ -690,7 +686,7 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const void *stack,
     }
     const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
     for (int y = 0; y <= kBlkSegLog; y++) { s1[o + y] = S1[y]; s2[o + y] = S2[y]; }
-    segsum[(size_t)pix * nbseg + seg] = (j1 - j0 == kBlkSeg) ? segv : nanf("");
+    segsum[(size_t)pix * nbseg + seg] = segv;     // used only for complete segments
 }
 
 // Blocking decision per pixel (one warp): combine segment statistics in FP64,
@@ -700,42 +696,45 @@ __global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, 
                                       const float *segsum, const float4 *blkmon, int *ind_out,
                                       int *ok_out)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ double shS1[4][kMaxBlockLevels], shS2[4][kMaxBlockLevels];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int pix = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (pix >= j.npix) return;
     const int blocknum = j.blocknum;
-    double S1[kMaxBlockLevels], S2[kMaxBlockLevels];
-    for (int y = 0; y < kMaxBlockLevels; y++) { S1[y] = 0.0; S2[y] = 0.0; }
-    for (int seg = lane; seg < nbseg; seg += 32) {
-        const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
-        for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) {
-            S1[y] += s1[o + y];
-            S2[y] += s2[o + y];
+    double *S1 = shS1[wib], *S2 = shS2[wib];
+    // levels inside a segment: lanes take segments, the warp reduces
+    for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) {
+        double a1 = 0.0, a2 = 0.0;
+        for (int seg = lane; seg < nbseg; seg += 32) {
+            const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
+            a1 += s1[o + y];
+            a2 += s2[o + y];
         }
+        a1 = warp_sum_d(a1);
+        a2 = warp_sum_d(a2);
+        if (lane == 0) { S1[y] = a1; S2[y] = a2; }
     }
-    for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) { S1[y] = warp_sum_d(S1[y]); S2[y] = warp_sum_d(S2[y]); }
     // levels above the segment: block y spans 2^(y-8) consecutive complete
     // segments; lanes take blocks, the warp reduces
+    const int full_segs = (j.num - 1) / kBlkSeg;   // segments holding kBlkSeg products
     for (int y = kBlkSegLog + 1; y < blocknum; y++) {
         const int span = 1 << (y - kBlkSegLog);
         const double inv = 1.0 / (double)(1 << y);
         double a1 = 0.0, a2 = 0.0;
-        for (int b = lane; (b + 1) * span <= nbseg; b += 32) {
+        for (int b = lane; (b + 1) * span <= full_segs; b += 32) {
+            // a block of complete segments (a non-finite segment sum, from a
+            // non-finite frame, propagates like the Java sums)
             double s = 0.0;
-            bool complete = true;
-            for (int k = 0; k < span; k++) {
-                float v = segsum[(size_t)pix * nbseg + b * span + k];
-                if (isnan(v)) { complete = false; break; }
-                s += (double)v;
-            }
-            if (!complete) continue;   // only the last block can be incomplete
+            for (int k = 0; k < span; k++) s += (double)segsum[(size_t)pix * nbseg + b * span + k];
             double m = s * inv;
             a1 += m;
             a2 += m * m;
         }
-        S1[y] = warp_sum_d(a1);
-        S2[y] = warp_sum_d(a2);
+        a1 = warp_sum_d(a1);
+        a2 = warp_sum_d(a2);
+        if (lane == 0) { S1[y] = a1; S2[y] = a2; }
     }
+    __syncwarp();
     if (lane != 0) return;
     const float4 bm = blkmon[pix];
     const double dmDm = (double)bm.z * (double)bm.w;
@@ -790,7 +789,7 @@ __global__ void center_given_kernel(Job j, const float *trace, float *bp_out)
     const float *y = trace + (size_t)tr * j.nopit;
     float bpl[kBleachStride];
     for (int i = 0; i < kBleachStride; i++) bpl[i] = bp[i];
-    float s = 0.f, lb[kMaxPoly + 1];
+    float s = 0.f, cnt = 0.f, lb[kMaxPoly + 1];
     for (int x = lane; x < j.nopit; x += 32) {
         float v = __ldg(&y[x]);
         if (j.bleach != IMFCS_BLEACH_NONE && bpl[11] != 0.f) {
@@ -798,10 +797,11 @@ __global__ void center_given_kernel(Job j, const float *trace, float *bp_out)
             if (j.bleach == IMFCS_BLEACH_POLYNOMIAL) legendre(t * bpl[13] + bpl[14], j.poly_order, lb);
             v = bleach_correct(v, bleach_f(bpl, j.bleach, j.poly_order, t, lb), bpl[9], bpl[10]);
         }
-        s += v;
+        if (isfinite(v)) { s += v; cnt += 1.f; }
     }
     s = warp_sum(s);
-    if (lane == 0) bp[12] = s / j.nopit;
+    cnt = warp_sum(cnt);
+    if (lane == 0) bp[12] = cnt > 0.f ? s / cnt : 0.f;
 }
 
 // Stride-1 box-sum binning of a float stack (calc_binning, agpufitjni.cu:4560-4586).
@@ -876,30 +876,26 @@ cudaError_t launch_center_given(const Job &j, const float *trace, float *bparams
     return cudaGetLastError();
 }
 
-cudaError_t launch_monitor(const Job &j, const LagInfo *li_dev, const void *stack,
-                           const float *bparams, const float *basis, const int *snap_pos, int nseg,
-                           float2 *segtot, float2 *snap_part, float4 *mon, float4 *blkmon,
-                           cudaStream_t s)
+cudaError_t launch_monitor_finalize(const Job &j, const LagInfo *li_dev, const float *bparams, int nseg,
+                                    const float2 *segtot, const float2 *snap_part, const int *segbad,
+                                    const int *snap_bad, float4 *mon, float4 *blkmon, cudaStream_t s)
 {
-    dim3 grid((j.ntrace + 127) / 128, nseg);
-    monitor_kernel<<<grid, 128, 0, s>>>(j, stack, bparams, basis, snap_pos, nseg, segtot, snap_part);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
     const int wpb = 4;
-    size_t smem = (size_t)wpb * (nseg + 1 + 2 * j.nsnap) * sizeof(double);
+    size_t smem = (size_t)wpb * (nseg + 1 + 4 * j.nsnap) * sizeof(double);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(monitor_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    monitor_finalize_kernel<<<(j.npix + wpb - 1) / wpb, wpb * 32, smem, s>>>(j, li_dev, bparams, nseg,
-                                                                           segtot, snap_part, mon, blkmon);
+    monitor_finalize_kernel<<<(j.npix + wpb - 1) / wpb, wpb * 32, smem, s>>>(j, li_dev, bparams, nseg, segtot,
+                                                                           snap_part, segbad, snap_bad, mon,
+                                                                           blkmon);
     return cudaGetLastError();
 }
 
-cudaError_t launch_block(const Job &j, const void *stack, const float *bparams, const float *basis,
-                         const float4 *blkmon, int nbseg, float *s1, float *s2, float *segsum,
-                         int *ind, int *ok, cudaStream_t s)
+cudaError_t launch_block(const Job &j, const float *s0, const float4 *blkmon, int nbseg, float *s1, float *s2,
+                         float *segsum, int *ind, int *ok, cudaStream_t s)
 {
     dim3 grid((j.npix + 127) / 128, nbseg);
-    block_kernel<<<grid, 128, 0, s>>>(j, stack, bparams, basis, blkmon, nbseg, s1, s2, segsum);
+    const float *s0b = j.is_ccf ? s0 + (size_t)j.npix * j.num : s0;
+    block_kernel<<<grid, 128, 0, s>>>(j, s0, s0b, blkmon, nbseg, s1, s2, segsum);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     block_finalize_kernel<<<(j.npix * 32 + 127) / 128, 128, 0, s>>>(j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);

@@ -166,7 +166,7 @@ class Plan:
         except Exception:
             pass
 
-    STAGES = ("trace+bleach", "monitors", "blocking", "correlator", "gls", "fits")
+    STAGES = ("trace+bleach", "stream", "blocking", "correlator", "gls", "fits")
 
     def set_timing(self, enable: bool = True):
         check(self._L.imfcs_plan_set_timing(self._h, int(enable)), "imfcs_plan_set_timing")

@@ -245,8 +245,10 @@ IMFCS_API int imfcs_plan_kernel_launches(const imfcs_plan *plan);
  * execution records CUDA events around its stages on the execution stream;
  * imfcs_plan_stage_times() (after the stream is synchronised) returns the
  * durations in ms of the last execution: [0] averaged trace + bleach fit,
- * [1] monitors, [2] blocking transform, [3] correlator, [4] GLS covariance,
- * [5] fits.  Returns the number of stages written. */
+ * [1] the streaming pass over the raw stack (corrected level-0 stream and
+ * the lags' monitors), [2] blocking transform, [3] correlator (level pairs,
+ * top levels, G and variance), [4] GLS covariance, [5] fits.  Returns the
+ * number of stages written. */
 IMFCS_API int imfcs_plan_set_timing(imfcs_plan *plan, int enable);
 IMFCS_API int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max_stages);
 

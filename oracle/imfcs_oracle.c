@@ -379,6 +379,124 @@ static void expfit_model(const double *p, double *f, double *jac, void *vctx)
     }
 }
 
+/* u(k, t) = (1 - e^{-kt}) / k and its first two k-derivatives, stable for
+ * any sign of k (series in x = kt for |x| < 0.05). */
+static void exp_u3(double k, double t, double *u, double *uk, double *ukk)
+{
+    const double x = k * t;
+    if (fabs(x) < 0.05) {
+        /* u = t sum_m (-x)^m / (m+1)!,  u_k = -t^2 sum_m (m+1) (-x)^m / (m+2)!,
+         * u_kk = t^3 sum_m (m+1)(m+2) (-x)^m / (m+3)! */
+        double su = 0.0, sk = 0.0, skk = 0.0, p = 1.0, f1 = 1.0, f2 = 2.0, f3 = 6.0;
+        for (int m = 0; m < 12; m++) {
+            su += p / f1;
+            sk += (m + 1) * p / f2;
+            skk += (m + 1) * (m + 2) * p / f3;
+            p *= -x;
+            f1 *= (m + 2);
+            f2 *= (m + 3);
+            f3 *= (m + 4);
+        }
+        *u = t * su;
+        *uk = -t * t * sk;
+        *ukk = t * t * t * skk;
+        return;
+    }
+    const double e = exp(-x);
+    *u = (1.0 - e) / k;
+    *uk = (t * e - *u) / k;
+    *ukk = (-t * t * e - 2.0 * *uk) / k;
+}
+
+/* Newton polish in FP64 from an LM result to the least-squares minimum
+ * itself, in the rate form f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c
+ * (s_c = A_c k_c, k_c = 1/tau_c, f0 = C + sum A_c): the same curves as
+ * A e^{-t/tau} + C (java:13028-13085), but continuous through k = 0 (tau =
+ * infinity, where A and C diverge with opposite signs), so that a trace
+ * whose minimum lies at or beyond that valley (a non-decaying trace, k <= 0)
+ * reaches it; with the full Hessian of chi^2/2, H = J^T J - sum_i r_i d2f_i
+ * (the Gauss-Newton matrix alone does not contract on these large-residual
+ * problems).  Steps are taken while chi^2 does not increase and H is
+ * positive definite, until |h_j| <= 1e-12 (|p_j| + sigma_j).
+ * The reference's commons-math LM stops on relative cost / parameter
+ * tolerances of 1e-10, i.e. within about 1e-4 standard errors of the
+ * minimum, and its A, tau, C parameters cannot cross tau = infinity; where
+ * the bleach correction is ill-conditioned (an averaged trace of a few
+ * photons in Java's int division) its stopping point moves G by more than the
+ * parity tolerance, so parity is defined on the minimum, which this polish
+ * reaches.  (Deviation from the Java stopping point, stated here once.) */
+static void exp_newton_polish(const double *t, const double *y, int n, int two, double *res)
+{
+    const int nc = two ? 2 : 1, k = 1 + 2 * nc;
+    double p[5], f0 = res[two ? 4 : 2];
+    for (int c = 0; c < nc; c++) {
+        const double A = res[2 * c], tau = res[2 * c + 1];
+        if (!(isfinite(A) && isfinite(tau)) || tau == 0.0) return;
+        p[1 + 2 * c] = A / tau;              /* s = A k */
+        p[2 + 2 * c] = 1.0 / tau;            /* k */
+        f0 += A;
+    }
+    p[0] = f0;
+    double chi2 = 0.0;
+    for (int it = 0; it < 60; it++) {
+        double a[25] = {0}, g[5] = {0}, l[25], h[5], pn[5];
+        chi2 = 0.0;
+        for (int i = 0; i < n; i++) {
+            double f = p[0], jac[5], hs[5][5] = {{0}};
+            jac[0] = 1.0;
+            for (int c = 0; c < nc; c++) {
+                double u, uk, ukk;
+                exp_u3(p[2 + 2 * c], t[i], &u, &uk, &ukk);
+                f -= p[1 + 2 * c] * u;
+                jac[1 + 2 * c] = -u;
+                jac[2 + 2 * c] = -p[1 + 2 * c] * uk;
+                hs[1 + 2 * c][2 + 2 * c] = hs[2 + 2 * c][1 + 2 * c] = -uk;
+                hs[2 + 2 * c][2 + 2 * c] = -p[1 + 2 * c] * ukk;
+            }
+            const double r = y[i] - f;
+            chi2 += r * r;
+            for (int j = 0; j < k; j++) {
+                g[j] += jac[j] * r;
+                for (int m = 0; m < k; m++) a[j * k + m] += jac[j] * jac[m] - r * hs[j][m];
+            }
+        }
+        if (!isfinite(chi2)) break;
+        memcpy(l, a, sizeof(double) * k * k);
+        if (chol_inplace(l, k)) break;           /* not in the convex region */
+        chol_solve(l, k, g, h);
+        int small = 1;
+        for (int j = 0; j < k; j++) {
+            double e[5], col[5];
+            for (int m = 0; m < k; m++) e[m] = (m == j);
+            chol_solve(l, k, e, col);
+            const double sig = sqrt(fabs(col[j]) * chi2 / (n > k ? n - k : 1));
+            if (!(fabs(h[j]) <= 1e-12 * (fabs(p[j]) + sig))) small = 0;
+            pn[j] = p[j] + h[j];
+        }
+        double chi2n = 0.0;
+        for (int i = 0; i < n; i++) {
+            double f = pn[0];
+            for (int c = 0; c < nc; c++) {
+                double u, uk, ukk;
+                exp_u3(pn[2 + 2 * c], t[i], &u, &uk, &ukk);
+                f -= pn[1 + 2 * c] * u;
+            }
+            chi2n += SQR(y[i] - f);
+        }
+        if (!(isfinite(chi2n) && chi2n <= chi2)) break;
+        memcpy(p, pn, sizeof(double) * k);
+        if (small) break;
+    }
+    /* back to the reference's parameters: A = s / k, tau = 1 / k, C = f0 - sum A */
+    double C = p[0];
+    for (int c = 0; c < nc; c++) {
+        res[2 * c] = p[1 + 2 * c] / p[2 + 2 * c];
+        res[2 * c + 1] = 1.0 / p[2 + 2 * c];
+        C -= res[2 * c];
+    }
+    res[two ? 4 : 2] = C;
+}
+
 int imfcs_o_exp_fit(const double *y, const double *t, int n, double *res3)
 {
     expfit_ctx c = {t, n, 0};
@@ -387,6 +505,7 @@ int imfcs_o_exp_fit(const double *y, const double *t, int n, double *res3)
     res3[2] = 0.0;
     lm_info info;
     int st = lm_solve(expfit_model, &c, n, 3, y, NULL, res3, 100000, &info, NULL);
+    if (st != 2) exp_newton_polish(t, y, n, 0, res3);
     return st == 2;
 }
 
@@ -400,6 +519,7 @@ int imfcs_o_dexp_fit(const double *y, const double *t, int n, double *res5)
     res5[4] = 0.0;
     lm_info info;
     int st = lm_solve(expfit_model, &c, n, 5, y, NULL, res5, 100000, &info, NULL);
+    if (st != 2) exp_newton_polish(t, y, n, 1, res5);
     return st == 2;
 }
 

@@ -26,9 +26,22 @@ def run_both(stack, cfg):
     return gpu, ref
 
 
+def acf_scale(ref_acf):
+    """Per-pixel scale of the ACF tolerance: |G(lag 1)|, or, where lag 1 is
+    not finite (a non-finite frame in its windows), the largest finite |G|
+    of lags >= 1."""
+    a = np.abs(ref_acf[:, 1:])
+    g1 = a[:, 0]
+    alt = np.where(np.isfinite(a), a, 0.0).max(axis=1)
+    return np.where(np.isfinite(g1), g1, alt)[:, None]
+
+
 def acf_deviation(gpu, ref):
-    """max over pixels and lags >= 1 of |dG| / |G(lag 1)| (finite pixels)."""
+    """max over pixels and lags >= 1 of |dG| / scale (entries finite in the
+    reference; see acf_scale)."""
     a_g, a_r = gpu["acf"][:, 1:], ref["acf"][:, 1:]
-    scale = np.abs(ref["acf"][:, 1:2])
-    ok = np.all(np.isfinite(a_r), axis=1)
-    return float(np.max(np.abs(a_g[ok] - a_r[ok]) / scale[ok])) if ok.any() else 0.0
+    fin = np.isfinite(a_r)
+    if not fin.any():
+        return 0.0
+    dev = np.abs(a_g - a_r) / acf_scale(ref["acf"])
+    return float(np.max(dev[fin]))

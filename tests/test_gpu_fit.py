@@ -204,12 +204,12 @@ def test_reference_calc_acf_float_path():
                      bleach=oracle.BLEACH_POLY, poly_order=order, do_fit=False)
     g = acf.reshape(73, -1).T
     np.testing.assert_array_equal(blk[0].ravel(), ref["blocked_ind"])
-    # pixels whose polynomial bleach curve crosses zero are non-finite in both
+    # a polynomial bleach curve through zero makes exactly the lags whose
+    # windows hold such a frame non-finite, in both
+    np.testing.assert_array_equal(np.isfinite(g), np.isfinite(ref["acf"]))
     full = np.all(np.isfinite(ref["acf"]), axis=1)
     assert full.sum() >= 5
-    assert not np.any(np.isfinite(g[~full, 1]))
-    scale = np.abs(ref["acf"][full, 1:2])
-    assert np.max(np.abs(g[full, 1:] - ref["acf"][full, 1:]) / scale) <= ACF_TOL
+    assert acf_deviation({"acf": g}, ref) <= ACF_TOL
 
 
 def test_reference_binning_and_bleach_average():
@@ -323,7 +323,7 @@ def _fit_api_vs_oracle(par, cst, free, init, **kw):
             # the fitted value is near zero (flow components)
             tol = max(FIT_TOL * abs(r["params"][j]), 1e-4 * r["sigma"][list(idx).index(j)])
             assert abs(outp[i, j] - r["params"][j]) <= tol, (i, j, outp[i, j], r["params"][j])
-        assert abs(chi[i] - r["chi2"] * (npts - len(idx) - 1)) <= 1e-3 * chi[i]
+        assert abs(chi[i] - r["chi2"] * (npts - 1 - len(idx) - 1)) <= 1e-3 * chi[i]   # (fitend - fitstart) - K - 1
         checked += 1
     assert checked >= n // 2
     return checked
@@ -342,18 +342,24 @@ def test_model_spim_finite_sz():
     _fit_api_vs_oracle(par, _cst(sz=0.9e-6), ONE, [1, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0, 0])
 
 
-def test_model_flow_vx_vy():
-    par = [5.0, 1e-12, 4e-5, -2e-5, 0.001, 0, 0, 0, 0, 0, 0]
-    free = [1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0]
-    _fit_api_vs_oracle(par, _cst(), free, [4, 1.2e-12, 3e-5, -1e-5, 0, 0, 0, 0, 0, 0, 0], rel_noise=0.001)
+def test_model_flow():
+    # flow along x free (with vx and vy both free on square pixels the
+    # normal matrix is numerically singular: vy is not identifiable), and a
+    # held flow along y
+    par = [5.0, 1e-12, 2e-5, 0, 0.001, 0, 0, 0, 0, 0, 0]
+    free = [1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(), free, [4, 1.2e-12, 1.5e-5, 0, 0, 0, 0, 0, 0, 0, 0], rel_noise=0.001)
+    par = [5.0, 1e-12, 0, 1.5e-5, 0.001, 0, 0, 0, 0, 0, 0]
+    _fit_api_vs_oracle(par, _cst(), ONE, [1, 1e-12, 0, 1.5e-5, 0, 0, 0, 0, 0, 0, 0])
 
 
 def test_model_triplet_held_and_free():
-    par = [5.0, 2e-12, 0, 0, 0.001, 0, 0, 0, 0, 0.25, 2e-5]
-    held = [1.0, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0.25, 2e-5]
+    # a triplet time of a few lag times (1 ms frames), held and free
+    par = [5.0, 2e-12, 0, 0, 0.001, 0, 0, 0, 0, 0.3, 3e-3]
+    held = [1.0, 1e-12, 0, 0, 0, 0, 0, 0, 0, 0.3, 3e-3]
     _fit_api_vs_oracle(par, _cst(), ONE, held)
     free = [1, 1, 0, 0, 1, 0, 0, 0, 0, 1, 1]
-    _fit_api_vs_oracle(par, _cst(), free, [4, 1.5e-12, 0, 0, 0, 0, 0, 0, 0, 0.2, 3e-5], rel_noise=0.0005)
+    _fit_api_vs_oracle(par, _cst(), free, [4, 1.5e-12, 0, 0, 0, 0, 0, 0, 0, 0.2, 2e-3], rel_noise=0.0005)
 
 
 def test_model_two_components():
