@@ -131,8 +131,10 @@ __global__ void center_kernel(Job j, const float *trace, float *bp_out)
 //     f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c,
 // which stay well conditioned when a component is slow (k_c t << 1, where
 // the reference's A and C grow without bound while A + C stays finite) and
-// are continuous through k_c = 0 (tau = infinity), so a trace whose minimum
-// lies at or beyond that valley (k_c <= 0, a non-decaying trace) reaches it.
+// are continuous through k_c = 0 (tau = infinity): the fit is the
+// least-squares minimum over k_c >= 0 (a rate at its bound whose step points
+// below it is held there), whose linear limit stands for the reference's
+// A, tau, C stopping in the tau -> infinity valley.
 // Scaled variables t / tmax, y / ymax; one warp per trace.
 //   phase 1: FP32 Levenberg-Marquardt until the Gauss-Newton step is below
 //            1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
@@ -372,15 +374,25 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
     return warp_sum_d(c2d);
 }
 
-// The undamped (Gauss-)Newton step on A h = g.  Rates k may take either
-// sign: the rate form is continuous through k = 0 (tau = infinity), so a
-// non-decaying trace reaches its minimum (k <= 0) instead of a bound.
+// The undamped (Gauss-)Newton step on A h = g, with a rate at its bound
+// k = 0 held there (bit set in `fix`) when its step points below it.  The
+// rate form is continuous through k = 0 (tau = infinity), so a trace whose
+// minimum over k >= 0 is the linear limit reaches it exactly; the
+// reference's A, tau, C cannot cross tau = infinity either and stop in that
+// valley, on the k -> 0+ side.
 template <int K>
-__device__ __forceinline__ bool exp_newton_step(const float *A, const double *gd, float *h)
+__device__ __forceinline__ bool exp_newton_step(const float *A, const double *gd, const double *p, unsigned &fix,
+                                                float *h)
 {
+    constexpr int NC = (K - 1) / 2;
     float g[K];
     for (int a = 0; a < K; a++) g[a] = (float)gd[a];
-    return solve_scaled_k<K>(A, g, 0.f, 0u, h);
+    fix = 0;
+    bool ok = solve_scaled_k<K>(A, g, 0.f, 0u, h);
+    for (int c = 0; c < NC; c++)
+        if (p[2 + 2 * c] <= 0.0 && (!ok || h[2 + 2 * c] < 0.f)) fix |= 1u << (2 + 2 * c);
+    if (fix) ok = solve_scaled_k<K>(A, g, 0.f, fix, h);
+    return ok;
 }
 
 template <int K>
@@ -421,9 +433,11 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     int evals = 1;
     for (int it_n = 0; ok && it_n < 400; it_n++) {
         float h[K];
-        if (exp_newton_step<K>(A, g, h)) {
+        unsigned fix;
+        if (exp_newton_step<K>(A, g, p, fix, h)) {
             bool conv = true;
             for (int a = 0; a < K; a++) {
+                if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
                 conv = conv && fabsf(h[a]) <= 1e-6f * (float)fabs(p[a]) + 1e-4f * sig;
             }
@@ -431,13 +445,14 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         }
         float gf[K];
         for (int a = 0; a < K; a++) gf[a] = (float)g[a];
-        if (!solve_scaled_k<K>(A, gf, lambda, 0u, h)) {
+        if (!solve_scaled_k<K>(A, gf, lambda, fix, h)) {
             lambda *= 10.f;
             if (lambda > 1e10f) break;
             continue;
         }
         double pn[K];
         for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
+        for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
         float An[K * K];
         double gn[K];
         const double c2n = exp_normal<K>(y, n, dts, iy, pn, false, An, gn, lane);
@@ -460,14 +475,17 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         evals++;
         for (int it_n = 0; it_n < 20 && isfinite(chi2); it_n++) {
             float h[K];
-            if (!exp_newton_step<K>(A, g, h)) break;   // Hessian not positive definite
+            unsigned fix;
+            if (!exp_newton_step<K>(A, g, p, fix, h)) break;   // Hessian not positive definite
             bool conv = true;
             for (int a = 0; a < K; a++) {
+                if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
                 conv = conv && fabsf(h[a]) <= 1e-12f * (float)fabs(p[a]) + 1e-9f * sig;
             }
             double pn[K];
             for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
+            for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
             float An[K * K];
             double gn[K];
             const double c2n = exp_normal<K>(y, n, dts, iy, pn, true, An, gn, lane);
@@ -684,58 +702,55 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const float *s0a, con
             else segv = v;
         }
     }
-    const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
-    for (int y = 0; y <= kBlkSegLog; y++) { s1[o + y] = S1[y]; s2[o + y] = S2[y]; }
-    segsum[(size_t)pix * nbseg + seg] = segv;     // used only for complete segments
+    // [level][segment][pixel]: coalesced here and in the finaliser
+    for (int y = 0; y <= kBlkSegLog; y++) {
+        const size_t o = ((size_t)y * nbseg + seg) * j.npix + pix;
+        s1[o] = S1[y];
+        s2[o] = S2[y];
+    }
+    segsum[(size_t)seg * j.npix + pix] = segv;     // used only for complete segments
 }
 
-// Blocking decision per pixel (one warp): combine segment statistics in FP64,
-// build the levels above the segment size from segment sums, then the
-// overlap / monotonic-increase criteria of java:9339-9380.
+// Blocking decision, one thread per pixel: the segments' statistics
+// combined in FP64 (coalesced across pixels), the levels above the segment
+// size built from segment sums, then the overlap / monotonic-increase
+// criteria of java:9339-9380.
 __global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, const float *s2,
                                       const float *segsum, const float4 *blkmon, int *ind_out,
                                       int *ok_out)
 {
-    __shared__ double shS1[4][kMaxBlockLevels], shS2[4][kMaxBlockLevels];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int pix = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= j.npix) return;
     const int blocknum = j.blocknum;
-    double *S1 = shS1[wib], *S2 = shS2[wib];
-    // levels inside a segment: lanes take segments, the warp reduces
+    double S1[kMaxBlockLevels], S2[kMaxBlockLevels];
     for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) {
         double a1 = 0.0, a2 = 0.0;
-        for (int seg = lane; seg < nbseg; seg += 32) {
-            const size_t o = ((size_t)pix * nbseg + seg) * (kBlkSegLog + 1);
-            a1 += s1[o + y];
-            a2 += s2[o + y];
+        const float *p1 = s1 + (size_t)y * nbseg * j.npix + pix, *p2 = s2 + (size_t)y * nbseg * j.npix + pix;
+        for (int seg = 0; seg < nbseg; seg++) {
+            a1 += (double)__ldg(&p1[(size_t)seg * j.npix]);
+            a2 += (double)__ldg(&p2[(size_t)seg * j.npix]);
         }
-        a1 = warp_sum_d(a1);
-        a2 = warp_sum_d(a2);
-        if (lane == 0) { S1[y] = a1; S2[y] = a2; }
+        S1[y] = a1;
+        S2[y] = a2;
     }
     // levels above the segment: block y spans 2^(y-8) consecutive complete
-    // segments; lanes take blocks, the warp reduces
+    // segments (a non-finite segment sum, from a non-finite frame, propagates
+    // like the Java sums)
     const int full_segs = (j.num - 1) / kBlkSeg;   // segments holding kBlkSeg products
     for (int y = kBlkSegLog + 1; y < blocknum; y++) {
         const int span = 1 << (y - kBlkSegLog);
         const double inv = 1.0 / (double)(1 << y);
         double a1 = 0.0, a2 = 0.0;
-        for (int b = lane; (b + 1) * span <= full_segs; b += 32) {
-            // a block of complete segments (a non-finite segment sum, from a
-            // non-finite frame, propagates like the Java sums)
-            double s = 0.0;
-            for (int k = 0; k < span; k++) s += (double)segsum[(size_t)pix * nbseg + b * span + k];
-            double m = s * inv;
+        for (int b = 0; (b + 1) * span <= full_segs; b++) {
+            double sb = 0.0;
+            for (int k = 0; k < span; k++) sb += (double)__ldg(&segsum[(size_t)(b * span + k) * j.npix + pix]);
+            const double m = sb * inv;
             a1 += m;
             a2 += m * m;
         }
-        a1 = warp_sum_d(a1);
-        a2 = warp_sum_d(a2);
-        if (lane == 0) { S1[y] = a1; S2[y] = a2; }
+        S1[y] = a1;
+        S2[y] = a2;
     }
-    __syncwarp();
-    if (lane != 0) return;
     const float4 bm = blkmon[pix];
     const double dmDm = (double)bm.z * (double)bm.w;
     const int nprod = j.num - 1;
@@ -898,7 +913,7 @@ cudaError_t launch_block(const Job &j, const float *s0, const float4 *blkmon, in
     block_kernel<<<grid, 128, 0, s>>>(j, s0, s0b, blkmon, nbseg, s1, s2, segsum);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    block_finalize_kernel<<<(j.npix * 32 + 127) / 128, 128, 0, s>>>(j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);
+    block_finalize_kernel<<<(j.npix + 127) / 128, 128, 0, s>>>(j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);
     return cudaGetLastError();
 }
 

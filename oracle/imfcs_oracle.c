@@ -408,39 +408,33 @@ static void exp_u3(double k, double t, double *u, double *uk, double *ukk)
     *ukk = (-t * t * e - 2.0 * *uk) / k;
 }
 
-/* Newton polish in FP64 from an LM result to the least-squares minimum
- * itself, in the rate form f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c
- * (s_c = A_c k_c, k_c = 1/tau_c, f0 = C + sum A_c): the same curves as
- * A e^{-t/tau} + C (java:13028-13085), but continuous through k = 0 (tau =
- * infinity, where A and C diverge with opposite signs), so that a trace
- * whose minimum lies at or beyond that valley (a non-decaying trace, k <= 0)
- * reaches it; with the full Hessian of chi^2/2, H = J^T J - sum_i r_i d2f_i
- * (the Gauss-Newton matrix alone does not contract on these large-residual
- * problems).  Steps are taken while chi^2 does not increase and H is
- * positive definite, until |h_j| <= 1e-12 (|p_j| + sigma_j).
- * The reference's commons-math LM stops on relative cost / parameter
- * tolerances of 1e-10, i.e. within about 1e-4 standard errors of the
- * minimum, and its A, tau, C parameters cannot cross tau = infinity; where
- * the bleach correction is ill-conditioned (an averaged trace of a few
- * photons in Java's int division) its stopping point moves G by more than the
- * parity tolerance, so parity is defined on the minimum, which this polish
- * reaches.  (Deviation from the Java stopping point, stated here once.) */
-static void exp_newton_polish(const double *t, const double *y, int n, int two, double *res)
+/* Exponential bleach fits in the rate form
+ *     f(t) = f0 - sum_c s_c (1 - e^{-k_c t}) / k_c,   k_c >= 0
+ * (s_c = A_c k_c, k_c = 1/tau_c, f0 = C + sum A_c): the same curves as the
+ * reference's A e^{-t/tau} + C (java:13028-13085), continuous through k = 0
+ * (tau = infinity, where A and C diverge with opposite signs; the linear
+ * limit f0 - s t).  The reference's LM moves in A, tau, C and cannot cross
+ * tau = infinity: on a trace whose least-squares minimum lies at or beyond
+ * that valley it stops in the valley, on the k -> 0+ side, at a point set by
+ * its stopping tolerances.  So the fit here is the least-squares minimum over
+ * k >= 0: the reference's LM from its initial values, then a Newton polish
+ * in the rate form with the full Hessian of chi^2/2, H = J^T J -
+ * sum_i r_i d2f_i (the Gauss-Newton matrix alone does not contract on these
+ * large-residual problems) and a rate held at 0 when its step points below
+ * (active set), while chi^2 does not increase and H is positive definite,
+ * until |h_j| <= 1e-12 (|p_j| + sigma_j).  The reference's commons-math LM
+ * stops on relative cost / parameter tolerances of 1e-10, i.e. within about
+ * 1e-4 standard errors of the minimum; where the bleach correction is
+ * ill-conditioned (an averaged trace of a few photons in Java's int
+ * division) that stopping point moves G by more than the parity tolerance,
+ * so parity is defined on the minimum.  (Deviation from the Java stopping
+ * point, stated here once.) */
+static void exp_rate_polish(const double *t, const double *y, int n, int nc, double *p)
 {
-    const int nc = two ? 2 : 1, k = 1 + 2 * nc;
-    double p[5], f0 = res[two ? 4 : 2];
-    for (int c = 0; c < nc; c++) {
-        const double A = res[2 * c], tau = res[2 * c + 1];
-        if (!(isfinite(A) && isfinite(tau)) || tau == 0.0) return;
-        p[1 + 2 * c] = A / tau;              /* s = A k */
-        p[2 + 2 * c] = 1.0 / tau;            /* k */
-        f0 += A;
-    }
-    p[0] = f0;
-    double chi2 = 0.0;
+    const int k = 1 + 2 * nc;
     for (int it = 0; it < 60; it++) {
         double a[25] = {0}, g[5] = {0}, l[25], h[5], pn[5];
-        chi2 = 0.0;
+        double chi2 = 0.0;
         for (int i = 0; i < n; i++) {
             double f = p[0], jac[5], hs[5][5] = {{0}};
             jac[0] = 1.0;
@@ -460,10 +454,28 @@ static void exp_newton_polish(const double *t, const double *y, int n, int two, 
                 for (int m = 0; m < k; m++) a[j * k + m] += jac[j] * jac[m] - r * hs[j][m];
             }
         }
-        if (!isfinite(chi2)) break;
-        memcpy(l, a, sizeof(double) * k * k);
-        if (chol_inplace(l, k)) break;           /* not in the convex region */
-        chol_solve(l, k, g, h);
+        if (!isfinite(chi2)) return;
+        int fix = 0;
+        for (int pass = 0; pass < 2; pass++) {
+            double aa[25], gg[5];
+            memcpy(aa, a, sizeof(aa));
+            memcpy(gg, g, sizeof(gg));
+            for (int j = 0; j < k; j++)
+                if ((fix >> j) & 1) {
+                    for (int m = 0; m < k; m++) aa[j * k + m] = aa[m * k + j] = 0.0;
+                    aa[j * k + j] = 1.0;
+                    gg[j] = 0.0;
+                }
+            memcpy(l, aa, sizeof(double) * k * k);
+            if (chol_inplace(l, k)) return;     /* not in the convex region */
+            chol_solve(l, k, gg, h);
+            int more = 0;
+            for (int c = 0; c < nc; c++) {
+                const int jk = 2 + 2 * c;
+                if (!((fix >> jk) & 1) && p[jk] <= 0.0 && h[jk] < 0.0) { fix |= 1 << jk; more = 1; }
+            }
+            if (!more) break;
+        }
         int small = 1;
         for (int j = 0; j < k; j++) {
             double e[5], col[5];
@@ -473,6 +485,7 @@ static void exp_newton_polish(const double *t, const double *y, int n, int two, 
             if (!(fabs(h[j]) <= 1e-12 * (fabs(p[j]) + sig))) small = 0;
             pn[j] = p[j] + h[j];
         }
+        for (int c = 0; c < nc; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
         double chi2n = 0.0;
         for (int i = 0; i < n; i++) {
             double f = pn[0];
@@ -483,44 +496,94 @@ static void exp_newton_polish(const double *t, const double *y, int n, int two, 
             }
             chi2n += SQR(y[i] - f);
         }
-        if (!(isfinite(chi2n) && chi2n <= chi2)) break;
+        if (!(isfinite(chi2n) && chi2n <= chi2)) return;
         memcpy(p, pn, sizeof(double) * k);
-        if (small) break;
+        if (small) return;
     }
-    /* back to the reference's parameters: A = s / k, tau = 1 / k, C = f0 - sum A */
-    double C = p[0];
-    for (int c = 0; c < nc; c++) {
-        res[2 * c] = p[1 + 2 * c] / p[2 + 2 * c];
-        res[2 * c + 1] = 1.0 / p[2 + 2 * c];
-        C -= res[2 * c];
+}
+
+/* The reference's LM (java:10862-10864, 10917-10921 initial values) and the
+ * rate-form polish; rate[] = f0, s1, k1 [, s2, k2].  Returns 0 on success. */
+static int exp_fit_rate(const double *y, const double *t, int n, int two, double *rate)
+{
+    expfit_ctx c = {t, n, two};
+    double res[5];
+    if (!two) {
+        res[0] = y[1];
+        res[1] = t[n / 2];
+        res[2] = 0.0;
+    } else {
+        res[0] = y[1] / 2;
+        res[1] = t[n / 10];
+        res[2] = y[1] / 2;
+        res[3] = t[n / 2];
+        res[4] = 0.0;
     }
-    res[two ? 4 : 2] = C;
+    lm_info info;
+    const int nc = two ? 2 : 1;
+    if (lm_solve(expfit_model, &c, n, 1 + 2 * nc, y, NULL, res, 100000, &info, NULL) == 2) return 1;
+    double f0 = res[two ? 4 : 2];
+    for (int m = 0; m < nc; m++) {
+        const double A = res[2 * m], tau = res[2 * m + 1];
+        if (!(isfinite(A) && isfinite(tau)) || tau == 0.0) return 1;
+        rate[1 + 2 * m] = A / tau;                 /* s = A k */
+        rate[2 + 2 * m] = fmax(1.0 / tau, 0.0);    /* k >= 0 */
+        f0 += A;
+    }
+    rate[0] = f0;
+    exp_rate_polish(t, y, n, nc, rate);
+    return 0;
+}
+
+/* rate form -> A, tau, C (tau = +inf, A = +-inf, C = -A for k = 0) */
+static void rate_to_reference(const double *rate, int nc, double *res)
+{
+    double C = rate[0];
+    for (int m = 0; m < nc; m++) {
+        const double s = rate[1 + 2 * m], k = rate[2 + 2 * m];
+        res[2 * m] = k > 0.0 ? s / k : copysign(INFINITY, s);
+        res[2 * m + 1] = k > 0.0 ? 1.0 / k : INFINITY;
+        C -= res[2 * m];
+    }
+    res[2 * nc] = C;
 }
 
 int imfcs_o_exp_fit(const double *y, const double *t, int n, double *res3)
 {
-    expfit_ctx c = {t, n, 0};
-    res3[0] = y[1];          /* java:10862-10864 */
-    res3[1] = t[n / 2];
-    res3[2] = 0.0;
-    lm_info info;
-    int st = lm_solve(expfit_model, &c, n, 3, y, NULL, res3, 100000, &info, NULL);
-    if (st != 2) exp_newton_polish(t, y, n, 0, res3);
-    return st == 2;
+    double rate[3];
+    if (exp_fit_rate(y, t, n, 0, rate)) return 1;
+    rate_to_reference(rate, 1, res3);
+    return 0;
 }
 
 int imfcs_o_dexp_fit(const double *y, const double *t, int n, double *res5)
 {
-    expfit_ctx c = {t, n, 1};
-    res5[0] = y[1] / 2;      /* java:10917-10921 */
-    res5[1] = t[n / 10];
-    res5[2] = y[1] / 2;
-    res5[3] = t[n / 2];
-    res5[4] = 0.0;
-    lm_info info;
-    int st = lm_solve(expfit_model, &c, n, 5, y, NULL, res5, 100000, &info, NULL);
-    if (st != 2) exp_newton_polish(t, y, n, 1, res5);
-    return st == 2;
+    double rate[5];
+    if (exp_fit_rate(y, t, n, 1, rate)) return 1;
+    rate_to_reference(rate, 2, res5);
+    return 0;
+}
+
+/* The exponential correction (java:9689-9692, 9714-9717) from rate-form
+ * parameters: f(t)/f0 with the curve continuous through k = 0.  The
+ * reference skips the correction when A tau (A1 tau1 A2 tau2) is 0, i.e.
+ * when a slope s is 0. */
+static void bleach_apply_rate(double *intdat, int num, double frametime, int nc, const double *rate)
+{
+    const double f0 = rate[0];
+    for (int m = 0; m < nc; m++)
+        if (rate[1 + 2 * m] == 0.0) return;
+    for (int x = 1; x <= num; x++) {
+        const double tt = frametime * (x + 0.5);
+        double f = f0;
+        for (int m = 0; m < nc; m++) {
+            double u, uk, ukk;
+            exp_u3(rate[2 + 2 * m], tt, &u, &uk, &ukk);
+            f -= rate[1 + 2 * m] * u;
+        }
+        const double r = f / f0;
+        intdat[x] = intdat[x] / sqrt(r) + f0 * (1 - sqrt(r));
+    }
 }
 
 void imfcs_o_bleach_apply(double *intdat, int num, double frametime, int mode, int order,
@@ -1205,10 +1268,14 @@ int imfcs_o_run(const imfcs_o_config *cfg, const uint16_t *stack, const int *bgr
                                         cfg->binx, cfg->biny, cfg->background, bgr, nopit,
                                         cfg->frametime, tr, tt);
                 int st = 0;
-                if (cfg->bleach == IMFCS_O_BLEACH_SINGLE_EXP) st = imfcs_o_exp_fit(tr, tt, nopit, res);
-                else if (cfg->bleach == IMFCS_O_BLEACH_DOUBLE_EXP) st = imfcs_o_dexp_fit(tr, tt, nopit, res);
-                else st = imfcs_o_poly_fit(tr, tt, nopit, cfg->poly_order, res);
-                if (!st) imfcs_o_bleach_apply(c, num, cfg->frametime, cfg->bleach, cfg->poly_order, res);
+                if (cfg->bleach == IMFCS_O_BLEACH_POLY) {
+                    st = imfcs_o_poly_fit(tr, tt, nopit, cfg->poly_order, res);
+                    if (!st) imfcs_o_bleach_apply(c, num, cfg->frametime, cfg->bleach, cfg->poly_order, res);
+                } else {
+                    const int two = cfg->bleach == IMFCS_O_BLEACH_DOUBLE_EXP;
+                    st = exp_fit_rate(tr, tt, nopit, two, res);
+                    if (!st) bleach_apply_rate(c, num, cfg->frametime, two ? 2 : 1, res);
+                }
             }
         }
         int bok = 0;
