@@ -159,9 +159,14 @@ def cpu_baseline(stack_np, cfg, sample_pixels, threads):
     return ncols * nrows / dt, ncols * nrows, dt, ref
 
 
-def parity_block(gpu, ref, n):
-    """GPU outputs of the first n pixels against the oracle's on the same pixels."""
+def parity_block(gpu, ref, n, sel=None):
+    """GPU outputs of the first n pixels against the oracle's on the same
+    pixels (restricted to the pixels `sel` when given)."""
     g = {k: v[:n] for k, v in gpu.items()}
+    if sel is not None:
+        g = {k: v[sel] for k, v in g.items()}
+        ref = {k: v[sel] for k, v in ref.items() if hasattr(v, "shape") and len(v) == n}
+        n = int(sel.sum())
     out = {"pixels": int(n)}
     out["blocked_ind_equal"] = int((g["blocked_ind"] == ref["blocked_ind"]).sum())
     out["blocked_ok_equal"] = int((g["blocked_ok"] == ref["blocked_ok"]).sum())
@@ -315,6 +320,19 @@ def main():
         cpu1_v, cpu1_n, cpu1_dt, _ = cpu_baseline(stack_np, cfg, min(sample, 256), 1)
         gpu_np = {k: v.cpu().numpy() for k, v in out.items()}
         parity = parity_block(gpu_np, ref, cpu_n)
+        if cfg.bleach in (_lib.BLEACH_SINGLE_EXP, _lib.BLEACH_DOUBLE_EXP):
+            # pixels whose exponential bleach rate the averaged trace does not
+            # determine (standard error >= the rate: a decay faster than the
+            # first averaged point, or a curve in the tau -> infinity valley):
+            # their least-squares minimum is flat along a curve, so the
+            # correction depends on where an optimiser stops
+            import oracle
+            ncols = min(cpu_n, W)
+            det = oracle.bleach_rate_determined(np.ascontiguousarray(stack_np[:, :cpu_n // ncols, :ncols]), ncols,
+                                                cpu_n // ncols, background=cfg.background, frametime=cfg.frametime,
+                                                two=cfg.bleach == _lib.BLEACH_DOUBLE_EXP)
+            parity["bleach_rate_undetermined"] = int((~det).sum())
+            parity["determined"] = parity_block(gpu_np, ref, cpu_n, det)
         fitted = int(out["fitted"].sum().item())
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

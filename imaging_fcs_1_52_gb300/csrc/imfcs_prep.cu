@@ -136,6 +136,9 @@ __global__ void center_kernel(Job j, const float *trace, float *bp_out)
 // below it is held there), whose linear limit stands for the reference's
 // A, tau, C stopping in the tau -> infinity valley.
 // Scaled variables t / tmax, y / ymax; one warp per trace.
+//   start:   single exponential: the global minimum over a grid of rates by
+//            variable projection (the oracle scans the same grid); double
+//            exponential: the reference's initial guesses;
 //   phase 1: FP32 Levenberg-Marquardt until the Gauss-Newton step is below
 //            1e-4 sigma + 1e-6 |p| (or no step lowers chi^2);
 //   phase 2: Newton with the full Hessian of chi^2/2 (J^T J - sum r d2f; the
@@ -413,13 +416,49 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     if (ym == 0.f) ym = 1.f;
     const float iy = 1.f / ym;
     double p[K];
-    {
-        // reference initial guesses (java:10862-10864, 10917-10921) in f0, s, k
+    if constexpr (K == 3) {
+        // global search by variable projection: for each rate of the grid
+        // x = k tmax in {0} and 96 log-spaced values 1e-3 .. 1e4 (the oracle's
+        // grid), c0 + c1 e^{-kt} (k = 0: c0 + c1 t) is linear in c0, c1 and
+        // chi^2 is minimised over them exactly; the best rate starts the LM
+        float sy = 0.f;
+        for (int x = lane; x < n; x += 32) sy += __ldg(&y[x]) * iy;
+        const float my = warp_sum(sy) / (float)n;
+        float syy = 0.f;
+        for (int x = lane; x < n; x += 32) { const float yc = __ldg(&y[x]) * iy - my; syy = fmaf(yc, yc, syy); }
+        syy = warp_sum(syy);
+        float bc = 3.4e38f, b0 = 0.f, b1 = 0.f, bk = 0.f;
+        for (int jg = 0; jg < 97; jg++) {
+            const float kx = jg == 0 ? 0.f : exp10f(-3.f + 7.f * (float)(jg - 1) / 95.f);
+            const float q = __expf(-kx * 32.f * dts);
+            const float e0 = __expf(-kx * ((float)lane + 0.5f) * dts);
+            float se = 0.f, e = e0;
+            for (int x = lane; x < n; x += 32) {
+                se += jg == 0 ? ((float)x + 0.5f) * dts : e;
+                e *= q;
+            }
+            const float me = warp_sum(se) / (float)n;
+            float see = 0.f, sye = 0.f;
+            e = e0;
+            for (int x = lane; x < n; x += 32) {
+                const float b = (jg == 0 ? ((float)x + 0.5f) * dts : e) - me;
+                see = fmaf(b, b, see);
+                sye = fmaf(__ldg(&y[x]) * iy - my, b, sye);
+                e *= q;
+            }
+            see = warp_sum(see);
+            sye = warp_sum(sye);
+            const float c1 = see > 0.f ? sye / see : 0.f;
+            const float c2 = syy - c1 * sye;
+            if (c2 < bc) { bc = c2; b1 = c1; b0 = my - c1 * me; bk = kx; }
+        }
+        if (bk == 0.f) { p[0] = b0; p[1] = -b1; p[2] = 0.0; }                  // f = c0 + c1 t
+        else { p[0] = (double)b0 + b1; p[1] = (double)b1 * bk; p[2] = bk; }       // f = c0 + c1 e^{-kt}
+    } else {
+        // reference initial guesses (java:10917-10921) in f0, s, k
         const double y1 = (double)__ldg(&y[1]) * (double)iy;
         const double thalf = ((double)(n / 2) + 0.5) * (double)dts;
-        if (K == 3) {
-            p[0] = y1; p[1] = y1 / thalf; p[2] = 1.0 / thalf;
-        } else {
+        {
             const double t10 = ((double)(n / 10) + 0.5) * (double)dts;
             p[0] = y1; p[1] = 0.5 * y1 / t10; p[2] = 1.0 / t10; p[3] = 0.5 * y1 / thalf; p[4] = 1.0 / thalf;
         }
@@ -431,7 +470,7 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     double chi2 = exp_normal<K>(y, n, dts, iy, p, false, A, g, lane);
     const bool ok = isfinite(chi2);
     int evals = 1;
-    for (int it_n = 0; ok && it_n < 400; it_n++) {
+    for (int it_n = 0; ok && it_n < 100; it_n++) {
         float h[K];
         unsigned fix;
         if (exp_newton_step<K>(A, g, p, fix, h)) {

@@ -77,6 +77,7 @@ def _declare(L):
     L.imfcs_o_poly_fit.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp]
     L.imfcs_o_exp_fit.argtypes = [_dp, _dp, C.c_int, _dp]
     L.imfcs_o_dexp_fit.argtypes = [_dp, _dp, C.c_int, _dp]
+    L.imfcs_o_exp_fit_rate.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp, _dp]
     L.imfcs_o_bleach_apply.argtypes = [_dp, C.c_int, C.c_double, C.c_int, C.c_int, _dp]
     L.imfcs_o_block_transform.restype = C.c_int
     L.imfcs_o_block_transform.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int, _ip, _dp, _dp,
@@ -161,6 +162,34 @@ def dexp_fit(y, t):
     st = lib().imfcs_o_dexp_fit(np.ascontiguousarray(y, float), np.ascontiguousarray(t, float),
                                 len(y), res)
     return res, st
+
+
+def exp_fit_rate(y, t, two=False):
+    """Rate-form exponential fit (f0, s1, k1 [, s2, k2]) and standard errors."""
+    k = 5 if two else 3
+    rate, sig = np.zeros(k), np.zeros(k)
+    st = lib().imfcs_o_exp_fit_rate(np.ascontiguousarray(y, float), np.ascontiguousarray(t, float), len(y),
+                                    int(two), rate, sig)
+    return rate, sig, st
+
+
+def bleach_rate_determined(stack, out_w, out_h, *, binx=1, biny=1, cfx=0, cfy=0, background=0,
+                           frametime=1e-3, two=False):
+    """Per output pixel: True where every exponential bleach rate of its
+    trace(s) is determined by the averaged trace (standard error below the
+    rate's value).  Elsewhere the least-squares minimum is flat along a curve
+    and the correction depends on where an optimiser stops."""
+    out = np.ones(out_w * out_h, bool)
+    for p in range(out_w * out_h):
+        ox, oy = p % out_w, p // out_w
+        for dx, dy in ((0, 0), (cfx, cfy)) if (cfx or cfy) else ((0, 0),):
+            tr, tt = intensity_trace(stack, ox * binx + dx, oy * biny + dy, binx=binx, biny=biny,
+                                     bckg=background, frametime=frametime)
+            rate, sig, st = exp_fit_rate(tr, tt, two)
+            ks = rate[2::2]
+            if st != 0 or not np.all(sig[2::2] < np.abs(ks)):
+                out[p] = False
+    return out
 
 
 def bleach_apply(intdat, frametime, mode, res, order=0):

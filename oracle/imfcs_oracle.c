@@ -502,10 +502,75 @@ static void exp_rate_polish(const double *t, const double *y, int n, int nc, dou
     }
 }
 
-/* The reference's LM (java:10862-10864, 10917-10921 initial values) and the
- * rate-form polish; rate[] = f0, s1, k1 [, s2, k2].  Returns 0 on success. */
+/* Global search for the single-exponential fit by variable projection: for a
+ * rate k the curve c0 + c1 e^{-kt} (k = 0: c0 + c1 t, the linear limit) is
+ * linear in c0, c1, so chi^2(k) is minimised over them exactly; k runs over
+ * a fixed grid, x = k tmax in {0} and 96 log-spaced values 1e-3 .. 1e4
+ * (tmax = the last averaged point's time), the best grid rate is refined by
+ * golden section between its neighbours.  The GPU path scans the same grid.
+ * Returns chi^2 at k and the linear parameters. */
+#define EXP_GRID 97
+static double exp_grid_x(int j) { return j == 0 ? 0.0 : pow(10.0, -3.0 + 7.0 * (j - 1) / 95.0); }
+
+static double varpro_chi2(const double *t, const double *y, int n, double k, double *c0, double *c1)
+{
+    double sy = 0.0, se = 0.0;
+    for (int i = 0; i < n; i++) {
+        sy += y[i];
+        se += k == 0.0 ? t[i] : exp(-k * t[i]);
+    }
+    const double my = sy / n, me = se / n;
+    double see = 0.0, sye = 0.0, syy = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double e = (k == 0.0 ? t[i] : exp(-k * t[i])) - me, yc = y[i] - my;
+        see += e * e;
+        sye += yc * e;
+        syy += yc * yc;
+    }
+    *c1 = see > 0.0 ? sye / see : 0.0;
+    *c0 = my - *c1 * me;
+    return syy - *c1 * sye;
+}
+
+/* Rate form (f0, s, k) of the global single-exponential minimum over k >= 0. */
+static void exp_fit_global(const double *t, const double *y, int n, double *rate)
+{
+    const double tmax = t[n - 1];
+    int best = 0;
+    double bc = INFINITY, c0, c1;
+    for (int j = 0; j < EXP_GRID; j++) {
+        const double c = varpro_chi2(t, y, n, exp_grid_x(j) / tmax, &c0, &c1);
+        if (c < bc) { bc = c; best = j; }
+    }
+    /* golden section on x between the neighbours of the best grid point */
+    double a = best > 0 ? exp_grid_x(best - 1) : 0.0;
+    double b = best < EXP_GRID - 1 ? exp_grid_x(best + 1) : exp_grid_x(best);
+    const double gr = 0.5 * (sqrt(5.0) - 1.0);
+    double x1 = b - gr * (b - a), x2 = a + gr * (b - a);
+    double f1 = varpro_chi2(t, y, n, x1 / tmax, &c0, &c1), f2 = varpro_chi2(t, y, n, x2 / tmax, &c0, &c1);
+    for (int it = 0; it < 200 && b - a > 1e-14 * (fabs(a) + fabs(b)) + 1e-300; it++) {
+        if (f1 <= f2) { b = x2; x2 = x1; f2 = f1; x1 = b - gr * (b - a); f1 = varpro_chi2(t, y, n, x1 / tmax, &c0, &c1); }
+        else { a = x1; x1 = x2; f1 = f2; x2 = a + gr * (b - a); f2 = varpro_chi2(t, y, n, x2 / tmax, &c0, &c1); }
+    }
+    double x = 0.5 * (a + b);
+    if (varpro_chi2(t, y, n, 0.0, &c0, &c1) <= varpro_chi2(t, y, n, x / tmax, &c0, &c1)) x = 0.0;
+    const double k = x / tmax;
+    varpro_chi2(t, y, n, k, &c0, &c1);
+    if (k == 0.0) { rate[0] = c0; rate[1] = -c1; rate[2] = 0.0; }      /* f = c0 + c1 t */
+    else { rate[0] = c0 + c1; rate[1] = c1 * k; rate[2] = k; }           /* f = c0 + c1 e^{-kt} */
+}
+
+/* rate[] = f0, s1, k1 [, s2, k2].  Single exponential: the global minimum
+ * over k >= 0 (variable projection on the rate grid), polished.  Double
+ * exponential: the reference's LM from its initial values (java:10917-10921)
+ * and the rate-form polish.  Returns 0 on success. */
 static int exp_fit_rate(const double *y, const double *t, int n, int two, double *rate)
 {
+    if (!two) {
+        exp_fit_global(t, y, n, rate);
+        exp_rate_polish(t, y, n, 1, rate);
+        return (isfinite(rate[0]) && isfinite(rate[1]) && isfinite(rate[2])) ? 0 : 1;
+    }
     expfit_ctx c = {t, n, two};
     double res[5];
     if (!two) {
@@ -546,6 +611,45 @@ static void rate_to_reference(const double *rate, int nc, double *res)
         C -= res[2 * m];
     }
     res[2 * nc] = C;
+}
+
+/* The rate-form fit (f0, s1, k1 [, s2, k2]) and the standard errors of its
+ * parameters, sqrt(diag((J^T J)^-1) chi2 / (n - k)) at the solution: a rate
+ * whose standard error is at least its value is not determined by the trace
+ * (a decay faster than the first averaged point, fitted to one non-zero
+ * point, or a curve in the tau -> infinity valley), so where an optimiser
+ * stops on it is arbitrary.  Returns 0 on success. */
+int imfcs_o_exp_fit_rate(const double *y, const double *t, int n, int two, double *rate, double *sigma)
+{
+    if (exp_fit_rate(y, t, n, two, rate)) return 1;
+    const int nc = two ? 2 : 1, k = 1 + 2 * nc;
+    double a[25] = {0}, l[25], chi2 = 0.0;
+    for (int i = 0; i < n; i++) {
+        double f = rate[0], jac[5];
+        jac[0] = 1.0;
+        for (int c = 0; c < nc; c++) {
+            double u, uk, ukk;
+            exp_u3(rate[2 + 2 * c], t[i], &u, &uk, &ukk);
+            f -= rate[1 + 2 * c] * u;
+            jac[1 + 2 * c] = -u;
+            jac[2 + 2 * c] = -rate[1 + 2 * c] * uk;
+        }
+        chi2 += SQR(y[i] - f);
+        for (int j = 0; j < k; j++)
+            for (int m = 0; m < k; m++) a[j * k + m] += jac[j] * jac[m];
+    }
+    memcpy(l, a, sizeof(l));
+    if (chol_inplace(l, k)) {
+        for (int j = 0; j < k; j++) sigma[j] = INFINITY;
+        return 0;
+    }
+    for (int j = 0; j < k; j++) {
+        double e[5], col[5];
+        for (int m = 0; m < k; m++) e[m] = (m == j);
+        chol_solve(l, k, e, col);
+        sigma[j] = sqrt(fabs(col[j]) * chi2 / (n > k ? n - k : 1));
+    }
+    return 0;
 }
 
 int imfcs_o_exp_fit(const double *y, const double *t, int n, double *res3)

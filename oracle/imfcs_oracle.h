@@ -56,6 +56,10 @@ int imfcs_o_poly_fit(const double *y, const double *t, int n, int order, double 
 int imfcs_o_exp_fit(const double *y, const double *t, int n, double *res3);
 int imfcs_o_dexp_fit(const double *y, const double *t, int n, double *res5);
 
+/* Exponential fits in the rate form f0 - sum s_c (1 - e^{-k_c t}) / k_c,
+ * k_c >= 0, with the standard errors of (f0, s1, k1 [, s2, k2]). */
+int imfcs_o_exp_fit_rate(const double *y, const double *t, int n, int two, double *rate, double *sigma);
+
 /* Correction of the 1-based trace (java:9682-9769). */
 void imfcs_o_bleach_apply(double *intdat, int num, double frametime, int mode,
                           int order, const double *res);
