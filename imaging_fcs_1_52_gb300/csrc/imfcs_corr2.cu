@@ -577,9 +577,11 @@ __global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const flo
 // ---------------------------------------------------------------------------
 __global__ void c2_finalize_kernel(C2Args a)
 {
+    // lag-major threads: the segment statistics [lag][stat][pixel] are read
+    // coalesced (they are most of this kernel's traffic)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.npix * a.chanum) return;
-    const int pix = i / a.chanum, lag = i % a.chanum;
+    const int lag = i / a.npix, pix = i % a.npix;
     const int ind = a.blk_ind[pix];
     const int pnum = a.li->pnum_by_ind[ind];
     const int level = lag <= kP ? 0 : 1 + (lag - (kP + 1)) / 8;

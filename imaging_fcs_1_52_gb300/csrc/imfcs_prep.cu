@@ -705,6 +705,7 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const float *s0a, con
     const int nprod = j.num - 1;
     const int j0 = seg * kBlkSeg, j1 = min(j0 + kBlkSeg, nprod);
     float S1[kBlkSegLog + 1], S2[kBlkSegLog + 1], pend[kBlkSegLog + 1];
+#pragma unroll
     for (int y = 0; y <= kBlkSegLog; y++) { S1[y] = 0.f; S2[y] = 0.f; pend[y] = 0.f; }
     // direct element of product jj is J_jj = v_{jj-1} (J_0 = 0); s0 holds the
     // corrected values centred on c, so J - dm1 = s0 - (dm1 - c)
@@ -728,20 +729,29 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const float *s0a, con
             const int rel = jj - j0;
             S1[0] += p;
             S2[0] += p * p;
+            // pairwise block means: level y+1 completes when bit y of rel is
+            // set; unrolled so that every array index is a constant (registers)
             float v = p;
-            int y = 0;
-            while (y < kBlkSegLog && ((rel >> y) & 1)) {
-                v = pend[y] + v;
-                y++;
-                float m = v * (1.f / (float)(1 << y));
-                S1[y] += m;
-                S2[y] += m * m;
+            bool carry = true;
+#pragma unroll
+            for (int y = 0; y < kBlkSegLog; y++) {
+                if (carry) {
+                    if ((rel >> y) & 1) {
+                        v = pend[y] + v;
+                        const float m = v * (1.f / (float)(1 << (y + 1)));
+                        S1[y + 1] += m;
+                        S2[y + 1] += m * m;
+                    } else {
+                        pend[y] = v;
+                        carry = false;
+                    }
+                }
             }
-            if (y < kBlkSegLog) pend[y] = v;
-            else segv = v;
+            if (carry) segv = v;
         }
     }
     // [level][segment][pixel]: coalesced here and in the finaliser
+#pragma unroll
     for (int y = 0; y <= kBlkSegLog; y++) {
         const size_t o = ((size_t)y * nbseg + seg) * j.npix + pix;
         s1[o] = S1[y];

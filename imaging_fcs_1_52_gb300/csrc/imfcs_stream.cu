@@ -7,10 +7,10 @@
 // windows need, and the count of non-finite frames) in the same pass.
 //
 // Staging: one CTA covers 32*NW consecutive output pixels of one output row
-// and one monitor segment of kSeg = 256 frames.  Its raw frames arrive as
-// four TMA boxes [64 frames][bh rows][bw columns] (cp.async.bulk.tensor),
-// all issued at once by one thread, each completing on its own mbarrier; the
-// threads (one per pixel) walk the staged frames in order.  Geometries TMA
+// and kStSegs monitor segments of kSeg = 256 frames.  Its raw frames arrive
+// as TMA boxes [64 frames][bh rows][bw columns] (cp.async.bulk.tensor) in a
+// ring of kStRing buffers, each completing on its own mbarrier; the threads
+// (one per pixel) walk the staged frames in order.  Geometries TMA
 // cannot take (float input, a row stride or base not 16-byte aligned, a box
 // wider than 256) read the raw frames with plain loads instead.
 //
@@ -33,7 +33,8 @@
 namespace imfcs {
 
 constexpr int kStF = 64;                       // frames per TMA box
-constexpr int kStBoxes = kSeg / kStF;          // boxes per CTA (one monitor segment)
+constexpr int kStRing = 3;                     // boxes in flight / being processed per CTA
+constexpr int kStSegs = 4;                     // monitor segments per CTA
 static_assert(kSeg % kStF == 0, "monitor segments must hold whole boxes");
 
 struct StreamArgs {
@@ -146,16 +147,22 @@ struct MonAcc {
     }
 };
 
-// TMA-staged stream pass: grid (tiles_x * out_h, nseg), 32 * nw threads.
+// TMA-staged stream pass: grid (tiles_x * out_h, ceil(nseg / kStSegs)),
+// 32 * nw threads.  A CTA walks kStSegs monitor segments (kStSegs * kSeg
+// frames) through a ring of kStRing boxes: while one box is processed the
+// next ones are in flight; a CTA barrier frees a box before thread 0 reloads
+// it.  The outcome of every bounded wait is made uniform across the CTA
+// (__syncthreads_or), so no thread is left waiting at a barrier.
 template <int MODE, bool CCF>
 __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     extern __shared__ __align__(128) unsigned char ssm[];
-    __shared__ uint64_t full[kStBoxes];
+    __shared__ uint64_t full[kStRing];
     const Job &j = a.j;
     const int nt = 32 * a.nw, tid = threadIdx.x;
     const int row = blockIdx.x / a.tiles_x, ox0 = (blockIdx.x % a.tiles_x) * nt;
-    const int seg = blockIdx.y, t0 = seg * kSeg, t1 = min(t0 + kSeg, j.num);
+    const int seg0 = blockIdx.y * kStSegs, seg1 = min(seg0 + kStSegs, a.nseg);
+    const int t0 = seg0 * kSeg, t1 = min(seg1 * kSeg, j.num);
     const int box = kStF * a.bh * a.bw;
     uint16_t *tiles = (uint16_t *)ssm;
     const int rx0 = (j.map_x0 + ox0) * j.pixbinx + min(0, j.cfx);
@@ -163,8 +170,8 @@ __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __g
     const int tx0 = rx0 & ~7, xoff = rx0 - tx0;       // x rounded down to 16 bytes
     const int nbox = (t1 - t0 + kStF - 1) / kStF;
     if (tid == 0) {
-        for (int b = 0; b < nbox; b++) mbar_init(&full[b], 1);
-        for (int b = 0; b < nbox; b++)
+        for (int b = 0; b < kStRing; b++) mbar_init(&full[b], 1);
+        for (int b = 0; b < nbox && b < kStRing; b++)
             tma_load_box(&tmap, tiles + (size_t)b * box, &full[b], tx0, ry0, j.first + t0 + b * kStF,
                          (uint32_t)box * 2);
     }
@@ -179,48 +186,58 @@ __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __g
     ca.load(a.bparams + (size_t)pix * kBleachStride, j.frametime);
     if (CCF) cb.load(a.bparams + (size_t)(j.npix + pix) * kBleachStride, j.frametime);
     MonAcc ma, mb;
-    ma.init(a, t0);
-    if (CCF) mb.init(a, t0);
-    bool ok = true;
+    int issued = nbox < kStRing ? nbox : kStRing;
     for (int b = 0; b < nbox; b++) {
-        if (!mbar_wait(&full[b], 0)) {
-            ok = false;
-            atomicExch(a.err, 1);
-            break;
+        const int slot = b % kStRing;
+        const bool waited = mbar_wait(&full[slot], (uint32_t)((b / kStRing) & 1));
+        if (__syncthreads_or(!waited)) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                // the copies still in flight land before the CTA leaves
+                for (int q = b; q < issued; q++) mbar_wait(&full[q % kStRing], (uint32_t)((q / kStRing) & 1));
+            }
+            return;
         }
-        if (!valid) continue;
         const int tb = t0 + b * kStF;
-        ca.seed(tb, j.frametime);
-        if (CCF) cb.seed(tb, j.frametime);
-        const uint16_t *fa = tiles + (size_t)b * box + ya * a.bw + xa;
-        const uint16_t *fb = tiles + (size_t)b * box + yb * a.bw + xb;
-        const int n = min(kStF, t1 - tb);
-        for (int f = 0; f < n; f++) {
-            const int t = tb + f;
-            int wa = 0, wb = 0;
-            for (int k = 0; k < j.biny; k++)
-                for (int i = 0; i < j.binx; i++) {
-                    wa += (int)fa[f * a.bh * a.bw + k * a.bw + i];
-                    if (CCF) wb += (int)fb[f * a.bh * a.bw + k * a.bw + i];
+        const int seg = tb / kSeg;
+        if (valid) {
+            if (tb % kSeg == 0) {
+                ma.init(a, tb);
+                if (CCF) mb.init(a, tb);
+            }
+            ca.seed(tb, j.frametime);
+            if (CCF) cb.seed(tb, j.frametime);
+            const uint16_t *fa = tiles + (size_t)slot * box + ya * a.bw + xa;
+            const uint16_t *fb = tiles + (size_t)slot * box + yb * a.bw + xb;
+            const int n = min(kStF, t1 - tb);
+            for (int f = 0; f < n; f++) {
+                const int t = tb + f;
+                int wa = 0, wb = 0;
+                for (int k = 0; k < j.biny; k++)
+                    for (int i = 0; i < j.binx; i++) {
+                        wa += (int)fa[f * a.bh * a.bw + k * a.bw + i];
+                        if (CCF) wb += (int)fb[f * a.bh * a.bw + k * a.bw + i];
+                    }
+                const float va =
+                    ma.add(a, pix, t, ca.apply((float)(wa - bgsum), t, j.frametime, j.poly_order, a.basis));
+                a.s0a[(size_t)t * j.npix + pix] = va;
+                if (CCF) {
+                    const float vb = mb.add(a, j.npix + pix, t,
+                                            cb.apply((float)(wb - bgsum), t, j.frametime, j.poly_order, a.basis));
+                    a.s0b[(size_t)t * j.npix + pix] = vb;
                 }
-            const float va = ma.add(a, pix, t, ca.apply((float)(wa - bgsum), t, j.frametime, j.poly_order, a.basis));
-            a.s0a[(size_t)t * j.npix + pix] = va;
-            if (CCF) {
-                const float vb = mb.add(a, j.npix + pix, t,
-                                        cb.apply((float)(wb - bgsum), t, j.frametime, j.poly_order, a.basis));
-                a.s0b[(size_t)t * j.npix + pix] = vb;
+            }
+            if (tb + kStF >= min((seg + 1) * kSeg, t1)) {   // last box of the segment
+                ma.store(a, pix, seg);
+                if (CCF) mb.store(a, j.npix + pix, seg);
             }
         }
-    }
-    if (!ok) {
-        // the copies still in flight land before the CTA leaves
-        if (tid == 0)
-            for (int b = 0; b < nbox; b++) mbar_wait(&full[b], 0);
-        return;
-    }
-    if (valid) {
-        ma.store(a, pix, seg);
-        if (CCF) mb.store(a, j.npix + pix, seg);
+        __syncthreads();                                    // box `slot` is free
+        if (tid == 0 && b + kStRing < nbox) {
+            tma_load_box(&tmap, tiles + (size_t)slot * box, &full[slot], tx0, ry0,
+                         j.first + t0 + (b + kStRing) * kStF, (uint32_t)box * 2);
+            issued = b + kStRing + 1;
+        }
     }
 }
 
@@ -274,7 +291,7 @@ static StreamPlan stream_plan(const Job &j, const void *stack)
         int bw = 7 + (32 * nw - 1) * j.pixbinx + j.binx + abs(j.cfx);
         bw = (bw + 7) & ~7;
         const int bh = j.biny + abs(j.cfy);
-        const size_t smem = (size_t)kStBoxes * kStF * bw * bh * 2;
+        const size_t smem = (size_t)kStRing * kStF * bw * bh * 2;
         if (bw > 256 || bh > 256 || smem > 100 * 1024) continue;
         sp.ok = 1;
         sp.nw = nw;
@@ -296,7 +313,7 @@ static cudaError_t launch_stream_t(const StreamArgs &a, const StreamPlan &sp, co
         auto kern = stream_tma_kernel<MODE, CCF>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.smem);
         if (e != cudaSuccess) return e;
-        kern<<<dim3(sp.tiles_x * j.out_h, a.nseg), 32 * sp.nw, sp.smem, s>>>(a, *map);
+        kern<<<dim3(sp.tiles_x * j.out_h, (a.nseg + kStSegs - 1) / kStSegs), 32 * sp.nw, sp.smem, s>>>(a, *map);
     } else {
         stream_plain_kernel<MODE, CCF><<<dim3((j.npix + 127) / 128, a.nseg), 128, 0, s>>>(a);
     }
