@@ -29,6 +29,10 @@ EXPORTS = [
     "imfcs_plan_execute_host", "imfcs_diffusion_law", "imfcs_simulate", "imfcs_plan_bleach_params",
     "imfcs_plan_set_timing", "imfcs_plan_stage_times", "imfcs_plan_kernel_launches",
     "imfcs_fit_device_noalloc",
+    "imfcs_surrogate_param_count", "imfcs_surrogate_create", "imfcs_surrogate_destroy",
+    "imfcs_surrogate_get_params", "imfcs_surrogate_set_params", "imfcs_surrogate_features",
+    "imfcs_surrogate_gradients", "imfcs_surrogate_train", "imfcs_surrogate_predict",
+    "imfcs_plan_set_surrogate", "imfcs_plan_surrogate_stats",
 ]
 
 
@@ -115,6 +119,18 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_plan_kernel_launches.argtypes = [vp]
     L.imfcs_fit_device_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, C.c_int, vp, C.c_float, C.c_int, C.c_int,
                                            vp, vp, vp, vp, vp, vp, vp]
+    L.imfcs_surrogate_param_count.restype = C.c_size_t
+    L.imfcs_surrogate_param_count.argtypes = []
+    L.imfcs_surrogate_create.argtypes = [C.c_uint64, C.POINTER(C.c_void_p)]
+    L.imfcs_surrogate_destroy.argtypes = [vp]
+    L.imfcs_surrogate_get_params.argtypes = [vp, vp]
+    L.imfcs_surrogate_set_params.argtypes = [vp, vp]
+    L.imfcs_surrogate_features.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp]
+    L.imfcs_surrogate_gradients.argtypes = [vp, vp, vp, C.c_int, vp, dp]
+    L.imfcs_surrogate_train.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint64, vp, vp]
+    L.imfcs_surrogate_predict.argtypes = [vp, vp, C.c_int, vp, vp]
+    L.imfcs_plan_set_surrogate.argtypes = [vp, vp, C.c_int]
+    L.imfcs_plan_surrogate_stats.argtypes = [vp, ip, ip]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

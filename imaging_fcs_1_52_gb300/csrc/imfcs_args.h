@@ -29,6 +29,8 @@ struct FitArgs {
     int *out_state;
     int *out_iter;
     float *out_hess;         // [fit][k*k] J^T W J at the optimum (internal units) or nullptr
+    const int *todo;         // [fit]: 0 = leave this fit's outputs untouched; nullptr = fit all
+    int *counter;            // zeroed work counter: warps take fits dynamically; nullptr = static stride
 };
 
 struct EpilogueArgs {

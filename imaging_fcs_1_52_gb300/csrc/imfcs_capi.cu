@@ -255,6 +255,12 @@ struct imfcs_plan {
     int *bfit_state = nullptr, *bfit_iter = nullptr;
     // internal copies of outputs the fit needs
     double *acf_int = nullptr, *var_int = nullptr;
+    // surrogate-seeded fits (allocated when a surrogate is first attached)
+    imfcs_surrogate *sur = nullptr;
+    int sur_mode = 0;
+    float *sur_x = nullptr, *sur_pred = nullptr, *sur_init = nullptr, *plain_par = nullptr, *plain_chi2 = nullptr;
+    int *plain_state = nullptr, *sur_todo = nullptr, *sur_count = nullptr;
+    int *lm_counter = nullptr;   // LM work counter (dynamic fit scheduling)
     // host path buffers
     uint16_t *dstack = nullptr;
     imfcs_outputs dout;
@@ -429,6 +435,7 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
         AL(pl->fit_hess, np * IMFCS_NPARAM * IMFCS_NPARAM);
         AL(pl->fit_state, np);
         AL(pl->fit_iter, np);
+        AL(pl->lm_counter, 1);
     }
     if (cfg->bayes) {
         AL(pl->logp1, np);
@@ -501,10 +508,14 @@ extern "C" int imfcs_plan_destroy(imfcs_plan *plan)
 
 extern "C" size_t imfcs_plan_scratch_bytes(const imfcs_plan *plan) { return plan ? plan->bytes : 0; }
 
-// Runs one LM pass plus its epilogue over all pixels.
-static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const float *y, const float *w,
-                   const float *init, int k, const int *idx, float *fitres, float *chi2, int *fitted,
-                   int *iters, double *logp, float *par_scratch)
+// One LM pass over the plan's pixels (those with todo[pix] != 0 when todo is
+// given), from init[pix * init_stride] (internal units).
+struct LMOut {
+    float *par, *chi2, *hess;
+    int *state, *iters;
+};
+static int run_lm(imfcs_plan *pl, cudaStream_t s, const float *y, const float *w, const float *init,
+                  int init_stride, int k, const int *idx, const int *todo, const LMOut &o)
 {
     const imfcs_config &c = pl->cfg;
     FitArgs a;
@@ -521,18 +532,30 @@ static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const floa
     a.w = w;
     a.x = pl->fit_x;
     a.init = init;
-    a.init_stride = 0;
+    a.init_stride = init_stride;
     a.cst = nullptr;
     a.mc = model_const_from(c.cst);
     a.linv = c.gls ? pl->linv : nullptr;
-    a.out_par = par_scratch;
+    a.out_par = o.par;
     a.out_stride = IMFCS_NPARAM;
-    a.out_chi2 = pl->fit_chi2;
-    a.out_state = pl->fit_state;
-    a.out_iter = iters ? iters : pl->fit_iter;
-    a.out_hess = pl->fit_hess;
+    a.out_chi2 = o.chi2;
+    a.out_state = o.state;
+    a.out_iter = o.iters;
+    a.out_hess = o.hess;
+    a.todo = todo;
+    a.counter = pl->lm_counter;
     CK(launch_lm(a, pl->num_sms, s));
     pl->launches += 1;
+    return 0;
+}
+
+// The fit epilogue over the LM results in par_scratch / fit_chi2 /
+// fit_state / fit_hess: SI parameters, reduced chi^2, fitted flags, Bayes
+// terms.
+static int run_epilogue(imfcs_plan *pl, cudaStream_t s, const double *acf, int k, const int *idx,
+                        float *fitres, float *chi2, int *fitted, double *logp, const float *par_scratch)
+{
+    const imfcs_config &c = pl->cfg;
     EpilogueArgs e;
     memset(&e, 0, sizeof(e));
     e.npix = pl->npix;
@@ -555,11 +578,47 @@ static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const floa
     e.pre_ok = c.gls ? pl->gls_ok : nullptr;
     e.acf = acf;
     e.linv = pl->linv;
-    e.mc = a.mc;
+    e.mc = model_const_from(c.cst);
     e.lagtime = pl->lagtime;
     CK(launch_fit_epilogue(e, s));
     pl->launches += 1;
     return 0;
+}
+
+// Plain LM from the shared initial values plus the epilogue.
+static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const float *y, const float *w,
+                   const float *init, int k, const int *idx, float *fitres, float *chi2, int *fitted,
+                   int *iters, double *logp, float *par_scratch)
+{
+    const LMOut o{par_scratch, pl->fit_chi2, pl->fit_hess, pl->fit_state, iters ? iters : pl->fit_iter};
+    if (run_lm(pl, s, y, w, init, 0, k, idx, nullptr, o)) return 1;
+    return run_epilogue(pl, s, acf, k, idx, fitres, chi2, fitted, logp, par_scratch);
+}
+
+// Surrogate-seeded LM: features + MLP + per-pixel seeds, the seeded LM, the
+// refit decision (and in mode 2 the plain-LM judge), LM from the configured
+// initial values on the refit pixels, then the epilogue.
+static int run_fit_seeded(imfcs_plan *pl, cudaStream_t s, const double *acf, const double *var, const float *y,
+                          const float *w, float *fitres, float *chi2, int *fitted, int *iters)
+{
+    int *it_out = iters ? iters : pl->fit_iter;
+    CK(cudaMemsetAsync(pl->sur_count, 0, 2 * sizeof(int), s));
+    if (surrogate_seed(pl->sur, pl->npix, pl->chanum, pl->k, pl->idx, acf, var, pl->sur_x, pl->sur_pred,
+                       pl->fit_init, pl->sur_init, s))
+        return 1;
+    pl->launches += 7;   // features, BF16 inputs, 3 GEMMs, de-standardise, seeds
+    if (pl->sur_mode == 2) {
+        const LMOut judge{pl->plain_par, pl->plain_chi2, nullptr, pl->plain_state, nullptr};
+        if (run_lm(pl, s, y, w, pl->fit_init, 0, pl->k, pl->idx, nullptr, judge)) return 1;
+    }
+    const LMOut o{pl->fit_par, pl->fit_chi2, pl->fit_hess, pl->fit_state, it_out};
+    if (run_lm(pl, s, y, w, pl->sur_init, IMFCS_NPARAM, pl->k, pl->idx, nullptr, o)) return 1;
+    CK(launch_seed_select(pl->npix, pl->k, pl->idx, pl->fit_par, pl->fit_state, pl->fit_chi2,
+                          pl->sur_mode == 2 ? pl->plain_state : nullptr, pl->sur_mode == 2 ? pl->plain_chi2 : nullptr,
+                          y, w, pl->nfitpts, pl->sur_todo, pl->sur_count, s));
+    pl->launches += 1;
+    if (run_lm(pl, s, y, w, pl->fit_init, 0, pl->k, pl->idx, pl->sur_todo, o)) return 1;
+    return run_epilogue(pl, s, acf, pl->k, pl->idx, fitres, chi2, fitted, nullptr, pl->fit_par);
 }
 
 namespace imfcs {
@@ -625,9 +684,14 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
         }
         if (c.do_fit) {
             if (!dev_out->fitres) { set_error("fitres output required when do_fit is set"); return 1; }
-            if (run_fit(pl, s, acf, y, w, pl->fit_init, pl->k, pl->idx, dev_out->fitres, dev_out->chi2,
-                        dev_out->fitted, dev_out->iterations, nullptr, pl->fit_par))
+            if (pl->sur && pl->sur_mode) {
+                if (run_fit_seeded(pl, s, acf, var, y, w, dev_out->fitres, dev_out->chi2, dev_out->fitted,
+                                   dev_out->iterations))
+                    return 1;
+            } else if (run_fit(pl, s, acf, y, w, pl->fit_init, pl->k, pl->idx, dev_out->fitres, dev_out->chi2,
+                               dev_out->fitted, dev_out->iterations, nullptr, pl->fit_par)) {
                 return 1;
+            }
         }
         if (c.bayes) {
             const int i1[3] = {0, 1, 4}, i2[5] = {0, 1, 4, 5, 6};
@@ -647,6 +711,53 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
     return 0;
 }
 }  // namespace imfcs
+
+extern "C" int imfcs_plan_set_surrogate(imfcs_plan *pl, imfcs_surrogate *sur, int mode)
+{
+    if (!pl) { set_error("null plan"); return 1; }
+    if (mode < 0 || mode > 2) { set_error("surrogate mode must be 0, 1 or 2"); return 1; }
+    if (!sur || mode == 0) {
+        pl->sur = nullptr;
+        pl->sur_mode = 0;
+        return 0;
+    }
+    if (!pl->cfg.do_fit) { set_error("the surrogate seeds the do_fit LM: enable do_fit"); return 1; }
+    if (pl->chanum < IMFCS_SURROGATE_INPUTS / 2 + 1) {
+        set_error("the surrogate reads lags 1..64: the plan needs at least 65 correlation channels");
+        return 1;
+    }
+    if (!pl->sur_x) {
+        const size_t np = pl->npix;
+        cudaError_t e = pl->alloc(pl->sur_x, np * IMFCS_SURROGATE_INPUTS);
+        if (e == cudaSuccess) e = pl->alloc(pl->sur_pred, np * IMFCS_SURROGATE_OUTPUTS);
+        if (e == cudaSuccess) e = pl->alloc(pl->sur_init, np * IMFCS_NPARAM);
+        if (e == cudaSuccess) e = pl->alloc(pl->plain_par, np * IMFCS_NPARAM);
+        if (e == cudaSuccess) e = pl->alloc(pl->plain_chi2, np);
+        if (e == cudaSuccess) e = pl->alloc(pl->plain_state, np);
+        if (e == cudaSuccess) e = pl->alloc(pl->sur_todo, np);
+        if (e == cudaSuccess) e = pl->alloc(pl->sur_count, 2);
+        if (e == cudaSuccess) e = cudaMemset(pl->sur_count, 0, 2 * sizeof(int));
+        if (e != cudaSuccess) {
+            pl->sur_x = nullptr;
+            set_error(cuda_msg(e, "surrogate buffers"));
+            return 1;
+        }
+    }
+    if (surrogate_reserve(sur, pl->npix)) return 1;
+    pl->sur = sur;
+    pl->sur_mode = mode;
+    return 0;
+}
+
+extern "C" int imfcs_plan_surrogate_stats(const imfcs_plan *pl, int *n_refit, int *n_worse)
+{
+    if (!pl) { set_error("null plan"); return 1; }
+    int c[2] = {0, 0};
+    if (pl->sur_count) CK(cudaMemcpy(c, pl->sur_count, sizeof(c), cudaMemcpyDeviceToHost));
+    if (n_refit) *n_refit = c[0];
+    if (n_worse) *n_worse = c[1];
+    return 0;
+}
 
 extern "C" int imfcs_plan_execute(imfcs_plan *pl, const uint16_t *dev_stack,
                                   const imfcs_outputs *dev_out, void *stream)

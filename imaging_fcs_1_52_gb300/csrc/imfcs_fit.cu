@@ -44,6 +44,10 @@ cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream)
     int blocks = (a.nfits + warps - 1) / warps;
     int cap = num_sms * 16;
     if (blocks > cap) blocks = cap;
+    if (a.counter) {
+        const cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), stream);
+        if (e != cudaSuccess) return e;
+    }
     if (km == 3) return launch_lm_k3(a, big, blocks, warps * 32, smem, stream);
     if (km == 5) return launch_lm_k5(a, big, blocks, warps * 32, smem, stream);
     return launch_lm_k11(a, big, blocks, warps * 32, smem, stream);

@@ -49,6 +49,21 @@ cudaError_t launch_binning(const float *in, float *out, int win, int hin, int wt
 cudaError_t launch_bleach_average(const float *in, float *out, int w, int h, int nopit, int ave,
                                   cudaStream_t s);
 
+// surrogate seeds (imfcs_mlp.cu): features, prediction and per-pixel LM
+// initial values init[pix][11] from the shared base_init (internal units)
+// (free parameters idx[0..k) only)
+int surrogate_seed(imfcs_surrogate *h, int npix, int chanum, int k, const int *idx, const double *acf,
+                   const double *var, float *x, float *pred, const float *base_init, float *init, cudaStream_t s);
+int surrogate_reserve(imfcs_surrogate *h, int n);   // work buffers for n pixels (allocates)
+// refit decision after a seeded LM: todo[pix] = 1 where the pixel's fit data
+// y/w [pix][npts] are finite and the seeded fit did not converge, ended with
+// N <= 0, D <= 0 or a non-finite free parameter, or (plain_chi2 given) its
+// chi^2 exceeds the converged plain chi^2 by > 1 %; counts[0] += refits,
+// counts[1] += the chi^2 cases
+cudaError_t launch_seed_select(int npix, int k, const int *idx, const float *par, const int *state,
+                               const float *chi2, const int *plain_state, const float *plain_chi2, const float *y,
+                               const float *w, int npts, int *todo, int *counts, cudaStream_t s);
+
 // error state
 void set_error(const std::string &msg);
 std::string cuda_msg(cudaError_t e, const char *what);

@@ -47,7 +47,7 @@ __device__ __forceinline__ ModelConstD to_double(const ModelConst &m)
 // Model value and gradient w.r.t. the free parameters at x.  precise: the
 // value comes from the FP64 model (ACF model); the gradient is always FP32.
 template <int KM>
-__device__ __forceinline__ double model_eval(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd,
+__device__ __noinline__ double model_eval(const FitArgs &a, const ModelConst &mc, const ModelConstD &mcd,
                                              const float *par, const double *pard, float x, float *gfree,
                                              bool c2, bool c3, bool precise)
 {
@@ -243,6 +243,16 @@ __device__ __forceinline__ bool solve_scaled(const float *A, const float *g, int
     return true;
 }
 
+// Next fit of a warp: a static stride over the fits, or, with a work counter,
+// the next unclaimed fit (so that warps whose fits converge early take more).
+__device__ __forceinline__ int lm_next_fit(const FitArgs &a, int fit, int nw, int lane)
+{
+    if (!a.counter) return fit + nw;
+    int f = 0;
+    if (lane == 0) f = atomicAdd(a.counter, 1);
+    return __shfl_sync(0xffffffffu, f, 0);
+}
+
 template <int KM, bool BIG>
 __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
 {
@@ -269,7 +279,8 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
         xl[m] = (!BIG && i < n) ? __ldg(&a.x[i]) : 0.f;
     }
 
-    for (int fit = gw; fit < a.nfits; fit += nw) {
+    for (int fit = a.counter ? lm_next_fit(a, 0, 0, lane) : gw; fit < a.nfits; fit = lm_next_fit(a, fit, nw, lane)) {
+        if (a.todo && !__ldg(&a.todo[fit])) continue;
         float yl[kPtsPerLane], wl[kPtsPerLane];
 #pragma unroll
         for (int m = 0; m < kPtsPerLane; m++) {
@@ -392,10 +403,15 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                 if (nprec > 60) { state = IMFCS_STATE_CONVERGED; it++; break; }
             }
             if (to_precise) {
-                // Newton steps on the FP64-residual gradient with the Hessian
-                // of chi^2/2, H = -dg/dp, from forward differences (0.1 sigma)
-                // of the FP32 gradient: converges in a few steps where
+                // Newton finish with the Hessian of chi^2/2, H = -dg/dp, from
+                // forward differences (0.1 sigma) of the FP32 gradient:
                 // Gauss-Newton contracts only linearly on a non-zero residual.
+                // (a) steps on the FP32-residual gradient to its stationary
+                //     point (cheap); (b) steps on the gradient of residuals
+                //     from the FP64 model value until the step is below
+                //     1e-4 sigma + 1e-7 |p| -- usually the first one, so one
+                //     FP64 evaluation per fit; the remaining error is about
+                //     the Hessian's relative error times that step.
                 float H[KM * KM];
 #pragma unroll
                 for (int i = 0; i < KM * KM; i++) H[i] = 0.f;
@@ -428,29 +444,39 @@ __global__ void __launch_bounds__(128) lm_kernel(FitArgs a)
                         H[r * KM + q] = v;
                         H[q * KM + r] = v;
                     }
-                bool newton_done = false;
+                bool newton_done = false, left = false;
 #pragma unroll 1
-                for (int ni = 0; ni < 4; ni++) {
-                    evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true,
-                                 yg, wg);
+                for (int ni = 0; ni < 7 && !left; ni++) {
+                    const bool fp64 = ni >= 3;   // (a) 3 FP32 steps at most, then (b)
+                    if (fp64) {
+                        evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3, true,
+                                     yg, wg);
+                        if (!isfinite(s.chi2)) { left = true; break; }
+                    }
                     float hn[KM];
-                    if (!isfinite(s.chi2) || !solve_scaled<KM>(H, s.g, a.k, 0.f, hn)) break;
-                    bool conv = true;
+                    if (!solve_scaled<KM>(H, s.g, a.k, 0.f, hn)) { left = true; break; }
+                    bool small = true;
 #pragma unroll
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) {
                             const float sig = rsqrtf(fmaxf(s.A[i * KM + i], 1e-30f));
-                            conv = conv && (fabsf(hn[i]) <= 1e-7f * fabsf(par[a.idx[i]]) + 1e-5f * sig);
-                            if (!(fabsf(hn[i]) <= 0.05f * sig)) ni = 4;   // not in the quadratic region
+                            if (!(fabsf(hn[i]) <= 0.05f * sig)) left = true;   // not in the quadratic region
+                            small = small && (fabsf(hn[i]) <= 1e-4f * sig + (fp64 ? 1e-7f * fabsf(par[a.idx[i]]) : 0.f));
                         }
-                    if (ni >= 4) break;
+                    if (left) break;
 #pragma unroll
                     for (int i = 0; i < KM; i++)
                         if (i < a.k) {
                             pard[a.idx[i]] += (double)hn[i];
                             par[a.idx[i]] = (float)pard[a.idx[i]];
                         }
-                    if (conv) { newton_done = true; break; }
+                    if (fp64 && small) { newton_done = true; break; }
+                    if (!fp64) {
+                        if (small) ni = 2;       // at the FP32 stationary point: go to (b)
+                        else
+                            evaluate<KM>(a, mc, mcd, par, pard, yl, wl, xl, lane, sh_fj, sh_f64, sh_linv, s, c2, c3,
+                                         false, yg, wg);
+                    }
                 }
                 if (newton_done) { state = IMFCS_STATE_CONVERGED; it++; break; }
                 // otherwise: Levenberg-Marquardt on the FP64-residual model

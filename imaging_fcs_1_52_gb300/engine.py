@@ -195,6 +195,22 @@ class Plan:
             raise _lib.ImfcsError(_lib.last_error())
         return out
 
+    def set_surrogate(self, surrogate, mode: int = 1):
+        """Seed the do_fit LM from a trained surrogate (imfcs_plan_set_surrogate):
+        mode 1 refits failed seeded fits from the configured initial values;
+        mode 2 also runs plain LM on every pixel and keeps the plain result
+        where the seeded chi^2 is more than 1 % higher; None / 0 detaches."""
+        h = None if surrogate is None else surrogate.handle
+        check(self._L.imfcs_plan_set_surrogate(self._h, h, int(mode if surrogate is not None else 0)),
+              "imfcs_plan_set_surrogate")
+        self._surrogate = surrogate   # keep the handle alive while attached
+
+    def surrogate_stats(self) -> dict:
+        """Refit counts of the last seeded execution (synchronises)."""
+        a, b = C.c_int(), C.c_int()
+        check(self._L.imfcs_plan_surrogate_stats(self._h, C.byref(a), C.byref(b)), "imfcs_plan_surrogate_stats")
+        return {"refit": int(a.value), "worse_than_plain": int(b.value)}
+
     def alloc_device_outputs(self, device="cuda"):
         import torch
         tmap = {"f8": torch.float64, "f4": torch.float32, "i4": torch.int32}

@@ -297,6 +297,62 @@ typedef struct imfcs_sim_params {
 IMFCS_API int imfcs_simulate(const imfcs_sim_params *sp, const float *dev_d_tile_map, uint16_t *dev_stack,
                    void *stream);
 
+/* ------------------------------------------------------------------------
+ * Learned fit seeds.  No counterpart in the reference, whose fits all start
+ * from the configured initial values (java:1958-1970, passed to the GPU fit
+ * at java:15112-15185).  A small MLP (128 -> 256 -> 256 -> 4, GELU, BF16
+ * tensor-core kernels with FP32 accumulation and FP32 master weights) maps
+ * a pixel's normalised ACF and its standard deviation, lags 1..64, to
+ * standardised predictions of log D [um^2/s], log(N G(1)), G_inf / G(1) and
+ * the fraction of a second component; a plan with a surrogate attached
+ * starts each pixel's LM fit from those predictions and refits from the
+ * configured initial values where the seeded fit fails (see
+ * imfcs_plan_set_surrogate).
+ * ---------------------------------------------------------------------- */
+typedef struct imfcs_surrogate imfcs_surrogate;
+#define IMFCS_SURROGATE_INPUTS 128
+#define IMFCS_SURROGATE_OUTPUTS 4
+/* Parameter count: W1[128][256] b1[256] W2[256][256] b2[256] W3[256][4] b3[4]
+ * (row-major, x W + b); the host parameter arrays of get/set_params hold
+ * these followed by the 4 target means and the 4 target standard deviations. */
+IMFCS_API size_t imfcs_surrogate_param_count(void);
+IMFCS_API int imfcs_surrogate_create(uint64_t seed, imfcs_surrogate **out);
+IMFCS_API int imfcs_surrogate_destroy(imfcs_surrogate *s);
+IMFCS_API int imfcs_surrogate_get_params(const imfcs_surrogate *s, float *host_params);
+IMFCS_API int imfcs_surrogate_set_params(imfcs_surrogate *s, const float *host_params);
+/* Inputs from correlator outputs (dev acf/var [npix][chanum], chanum >= 65):
+ * dev_x[npix][128] = G(i)/G(1) for i = 1..64, then sd(i)/|G(1)|. */
+IMFCS_API int imfcs_surrogate_features(int npix, int chanum, const double *dev_acf, const double *dev_var,
+                                       float *dev_x, void *stream);
+/* One forward + backward pass of the mean squared error against standardised
+ * targets ((t - mean) / std with the handle's current mean and std) over n
+ * samples: host_grads[param_count] (nullable) and *loss (nullable). */
+IMFCS_API int imfcs_surrogate_gradients(imfcs_surrogate *s, const float *dev_x, const float *dev_t, int n,
+                                        float *host_grads, double *loss);
+/* Adam training: sets the target standardisation from dev_t [n][4], then
+ * `steps` minibatch steps of `batch` consecutive samples at seeded random
+ * offsets (shuffle the samples beforehand).  loss_history[steps] nullable. */
+IMFCS_API int imfcs_surrogate_train(imfcs_surrogate *s, const float *dev_x, const float *dev_t, int n, int steps,
+                                    int batch, float learning_rate, uint64_t seed, float *loss_history,
+                                    void *stream);
+/* De-standardised predictions dev_out[n][4]. */
+IMFCS_API int imfcs_surrogate_predict(imfcs_surrogate *s, const float *dev_x, int n, float *dev_out, void *stream);
+
+/* Attaches a surrogate to a plan's do_fit LM (NULL or mode 0 detaches).
+ * mode 1: seeded LM, then LM from the configured initial values for every
+ *         pixel whose seeded fit did not converge or ended with N <= 0,
+ *         D <= 0 or a non-finite parameter;
+ * mode 2: as mode 1, and plain LM from the configured initial values also
+ *         runs for every pixel; a pixel whose seeded chi^2 exceeds the plain
+ *         chi^2 by more than 1 % takes the plain result (the plain fit is the
+ *         judge of the seeded one).
+ * The plan keeps the pointer; the surrogate must outlive its use. */
+IMFCS_API int imfcs_plan_set_surrogate(imfcs_plan *plan, imfcs_surrogate *s, int mode);
+/* After an execute with a surrogate attached (synchronise first): pixels
+ * refit from the configured initial values, and (mode 2) pixels whose
+ * seeded chi^2 exceeded the plain chi^2 by more than 1 %. */
+IMFCS_API int imfcs_plan_surrogate_stats(const imfcs_plan *plan, int *n_refit, int *n_worse);
+
 #ifdef __cplusplus
 }
 #endif
