@@ -229,6 +229,55 @@ def reference_arm(args):
     return 0
 
 
+def surrogate_block(plan, stack, steps):
+    """Surrogate-seeded LM against plain LM on the same correlator outputs:
+    fit-stage device time (features + MLP + seeded LM + refits in the seeded
+    mode), fitted pixels/s, and agreement at equal chi^2 (mode 1: refit of
+    failed seeded fits; mode 2: plain LM also runs and judges every pixel)."""
+    import torch
+    from imaging_fcs_1_52_gb300 import surrogate
+    if not os.path.exists(surrogate.DEFAULT_WEIGHTS):
+        return {"unavailable": "no trained weights (python -m imaging_fcs_1_52_gb300.train_surrogate)"}
+    sur = surrogate.Surrogate.load()
+
+    def run(mode):
+        plan.set_surrogate(sur if mode else None, mode)
+        o = plan.alloc_device_outputs()
+        plan.execute(stack, o)
+        ts = []
+        for _ in range(max(3, steps)):
+            plan.execute(stack, o)
+            torch.cuda.synchronize()
+            ts.append(plan.stage_times()["fits"])
+        st = plan.surrogate_stats() if mode else {}
+        return {k: v.cpu().numpy() for k, v in o.items()}, statistics.median(ts), st
+
+    p_np, p_ms, _ = run(0)
+    blk = {"weights": os.path.relpath(surrogate.DEFAULT_WEIGHTS, os.path.dirname(os.path.abspath(__file__))),
+           "training": sur.meta.get("data", {}).get("curves"),
+           "plain": {"fits_ms": p_ms, "fitted": int(p_np["fitted"].sum()),
+                     "fitted_pixels_per_s": float(p_np["fitted"].sum()) / (p_ms * 1e-3),
+                     "iterations_mean": float(p_np["iterations"].mean())}}
+    for mode in (1, 2):
+        s_np, s_ms, st = run(mode)
+        both = (p_np["fitted"] == 1) & (s_np["fitted"] == 1)
+        cr = s_np["chi2"][both] / p_np["chi2"][both]
+        d = {"fits_ms": s_ms, "fitted": int(s_np["fitted"].sum()),
+             "fitted_pixels_per_s": float(s_np["fitted"].sum()) / (s_ms * 1e-3),
+             "speedup_vs_plain": p_ms / s_ms, "iterations_mean": float(s_np["iterations"].mean()),
+             "refit": st.get("refit"), "worse_than_plain_refit": st.get("worse_than_plain"),
+             "fitted_equal": int((s_np["fitted"] == p_np["fitted"]).sum()), "fitted_both": int(both.sum()),
+             "chi2_within_1pct": int((cr <= 1.01).sum()), "chi2_ratio_max": float(cr.max()) if both.any() else None,
+             "chi2_ratio_min": float(cr.min()) if both.any() else None}
+        for i, nm in ((0, "N"), (1, "D")):
+            rel = np.abs(s_np["fitres"][both, i] / p_np["fitres"][both, i] - 1)
+            d[f"{nm}_rel_p99"] = float(np.quantile(rel, 0.99)) if both.any() else None
+            d[f"{nm}_over_1e-4"] = int((rel > 1e-4).sum())
+        blk[f"seeded_mode{mode}"] = d
+    plan.set_surrogate(None)
+    return blk
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -288,10 +337,14 @@ def main():
     host = torch.empty((T, H, W), dtype=torch.int16, pin_memory=True)
     host.copy_(torch.from_numpy(stack_np.view(np.int16)))
     host_np = host.numpy().view(np.uint16)
+    # results land in pinned host buffers (page-locked, as the stack): the
+    # device-to-host copies then run at link speed instead of through a
+    # pageable bounce buffer
     outs_host = {}
+    tdt = {"f8": torch.float64, "f4": torch.float32, "i4": torch.int32}
     for n in engine.output_names(cfg):
         dt, shp = engine._OUT_SPEC[n]
-        outs_host[n] = np.empty((cfg.npix, *shp(cfg.chanum)), dtype=dt)
+        outs_host[n] = torch.empty((cfg.npix, *shp(cfg.chanum)), dtype=tdt[dt], pin_memory=True).numpy()
     plan.execute_host(host_np, outs_host)           # warm-up of the host path
     barrier()
     t0 = time.perf_counter()
@@ -334,6 +387,7 @@ def main():
             parity["bleach_rate_undetermined"] = int((~det).sum())
             parity["determined"] = parity_block(gpu_np, ref, cpu_n, det)
         fitted = int(out["fitted"].sum().item())
+        sur_blk = surrogate_block(plan, stack, args.steps)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -360,6 +414,7 @@ def main():
                                            "sample": f"{cpu1_n} pixels x {T} frames, {cpu1_dt:.1f} s"},
             "clocks": clk.summary(),
             "parity": parity,
+            "surrogate": sur_blk,
         }
         print(json.dumps(line))
     if world > 1:

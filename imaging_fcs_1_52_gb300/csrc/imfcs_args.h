@@ -31,6 +31,7 @@ struct FitArgs {
     float *out_hess;         // [fit][k*k] J^T W J at the optimum (internal units) or nullptr
     const int *todo;         // [fit]: 0 = leave this fit's outputs untouched; nullptr = fit all
     int *counter;            // zeroed work counter: warps take fits dynamically; nullptr = static stride
+    int tirf_zero_held;      // the held parameters (vx, vy, F2, F3, Ftrip) are zero for every fit
 };
 
 struct EpilogueArgs {

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -261,6 +262,9 @@ struct imfcs_plan {
     float *sur_x = nullptr, *sur_pred = nullptr, *sur_init = nullptr, *plain_par = nullptr, *plain_chi2 = nullptr;
     int *plain_state = nullptr, *sur_todo = nullptr, *sur_count = nullptr;
     int *lm_counter = nullptr;   // LM work counter (dynamic fit scheduling)
+    int *bg_sums = nullptr;      // per-trace background sums [2][ntrace] (background image)
+    bool nb_only = false;        // N&B mode of the reference calcACF: lag 1 only
+    double *nb_sum = nullptr;    // its lag-1 product sums [npix]
     // host path buffers
     uint16_t *dstack = nullptr;
     imfcs_outputs dout;
@@ -544,6 +548,9 @@ static int run_lm(imfcs_plan *pl, cudaStream_t s, const float *y, const float *w
     a.out_hess = o.hess;
     a.todo = todo;
     a.counter = pl->lm_counter;
+    // held flow, second/third component and triplet fractions all zero: the
+    // default one-component model (seeds change only N, D, G)
+    a.tirf_zero_held = c.init[2] == 0 && c.init[3] == 0 && c.init[5] == 0 && c.init[7] == 0 && c.init[9] == 0;
     CK(launch_lm(a, pl->num_sms, s));
     pl->launches += 1;
     return 0;
@@ -647,6 +654,14 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
                                pl->snap_bad, pl->mon, pl->blkmon, s));
     pl->launches += 2;
     pl->mark(2, s);
+    if (pl->nb_only) {
+        // N&B mode: lag 1 only; the correlator, blocking and fits do not run
+        if (!pl->nb_sum) CK(pl->alloc(pl->nb_sum, pl->npix));
+        CK(launch_nb_lag1(j, pl->s0, pl->mon, pl->nb_sum, dev_out->nb_mean, dev_out->nb_cov, s));
+        pl->launches += 2;
+        for (int i = 3; i <= 6; i++) pl->mark(i, s);
+        return 0;
+    }
     CK(launch_block(j, pl->s0, pl->blkmon, pl->nbseg, pl->s1, pl->s2, pl->segsum, pl->blk_ind, pl->blk_ok, s));
     pl->launches += 2;
     pl->mark(3, s);
@@ -749,6 +764,48 @@ extern "C" int imfcs_plan_set_surrogate(imfcs_plan *pl, imfcs_surrogate *sur, in
     return 0;
 }
 
+extern "C" int imfcs_plan_set_background_image(imfcs_plan *pl, const double *host_bg)
+{
+    if (!pl) { set_error("null plan"); return 1; }
+    Job &j = pl->job;
+    if (j.input_float) { set_error("the float-stack path takes background-subtracted data"); return 1; }
+    if (!host_bg) {
+        j.bg_trace = nullptr;
+        j.bg_avg = nullptr;
+        return 0;
+    }
+    const size_t n = (size_t)j.in_w * j.in_h;
+    std::vector<int> r(n);
+    for (size_t i = 0; i < n; i++) {
+        const double v = host_bg[i];
+        if (!std::isfinite(v) || v < -2e9 || v > 2e9) { set_error("background image holds an invalid value"); return 1; }
+        r[i] = (int)std::floor(v + 0.5);   // Math.round
+    }
+    // per trace: its own window (values) and the direct window (averaged trace)
+    std::vector<int> sums((size_t)2 * j.ntrace);
+    for (int tr = 0; tr < j.ntrace; tr++) {
+        int x0, y0, xd, yd;
+        trace_origin(j, tr, x0, y0);
+        trace_origin(j, tr % j.npix, xd, yd);
+        long s = 0, sa = 0;
+        for (int k = 0; k < j.biny; k++)
+            for (int i = 0; i < j.binx; i++) {
+                s += r[(size_t)(y0 + k) * j.in_w + x0 + i];
+                sa += r[(size_t)(yd + k) * j.in_w + xd + i];
+            }
+        sums[tr] = (int)s;
+        sums[(size_t)j.ntrace + tr] = (int)sa;
+    }
+    if (!pl->bg_sums) {
+        cudaError_t e = pl->alloc(pl->bg_sums, sums.size());
+        if (e != cudaSuccess) { set_error(cuda_msg(e, "background image buffer")); return 1; }
+    }
+    CK(cudaMemcpy(pl->bg_sums, sums.data(), sums.size() * sizeof(int), cudaMemcpyHostToDevice));
+    j.bg_trace = pl->bg_sums;
+    j.bg_avg = pl->bg_sums + j.ntrace;
+    return 0;
+}
+
 extern "C" int imfcs_plan_surrogate_stats(const imfcs_plan *pl, int *n_refit, int *n_worse)
 {
     if (!pl) { set_error("null plan"); return 1; }
@@ -826,6 +883,7 @@ extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stac
 namespace imfcs {
 float *plan_bparams(imfcs_plan *pl) { return pl->bparams; }
 const Job &plan_job(imfcs_plan *pl) { return pl->job; }
+void plan_set_nb_only(imfcs_plan *pl, bool on) { pl->nb_only = on; }
 void plan_umap(imfcs_plan *pl, double &uscale, double &uoff)
 {
     // u-mapping of the averaged-trace time axis (same as legendre_projection)

@@ -225,13 +225,14 @@ __host__ __device__ inline size_t corr_smem_floats_dev(int q, bool ccf)
 // are bounded: on a timeout the CTA records an error and leaves.
 // ---------------------------------------------------------------------------
 // Window value of a trace from the staged raw tile (frame fr of the chunk).
-__device__ __forceinline__ float tile_value(const Job &j, const uint16_t *tile, int BW, int BH, int fr, int xr, int yr)
+__device__ __forceinline__ float tile_value(const Job &j, const uint16_t *tile, int BW, int BH, int fr, int xr, int yr,
+                                            int bg)
 {
     const uint16_t *f = tile + (size_t)fr * BH * BW;
     int acc = 0;
     for (int k = 0; k < j.biny; k++)
         for (int i = 0; i < j.binx; i++) acc += (int)f[(yr + k) * BW + xr + i];
-    return (float)(acc - j.background * j.binx * j.biny);
+    return (float)(acc - bg);
 }
 
 struct TmaGeom {
@@ -280,6 +281,7 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
     trace_origin(j, pixc, xa, ya);
     const int trb = CCF ? j.npix + pixc : pixc;
     trace_origin(j, trb, xb, yb);
+    const int bga = trace_bg(j, pixc), bgb = trace_bg(j, trb);
     // tile origin (x rounded down to 8 elements for TMA alignment)
     const int xt0 = (j.map_x0 + seg * 32) * j.pixbinx;
     const int yt0 = (j.map_y0 + oy) * j.pixbiny;
@@ -348,14 +350,14 @@ __global__ void __launch_bounds__(kCorrThreads) corr_kernel(Job j, const LagInfo
                 if (f < j.num && pvalid) {
                     float t = frame_time(j, f);
                     const float *bs = sh_basis + fr * order1;
-                    va = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xa - tx0, ya - ty0)
-                                    : window_value(j, stack, xa, ya, f);
+                    va = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xa - tx0, ya - ty0, bga)
+                                    : window_value(j, stack, xa, ya, f, bga);
                     if (j.bleach != IMFCS_BLEACH_NONE && bpa[11] != 0.f)
                         va = bleach_correct(va, bleach_f(bpa, j.bleach, j.poly_order, t, bs), bpa[9], bpa[10]);
                     va -= bpa[12];
                     if (CCF) {
-                        vb = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xb - tx0, yb - ty0)
-                                        : window_value(j, stack, xb, yb, f);
+                        vb = tg.use_tma ? tile_value(j, raw, tg.bw, tg.bh, fr, xb - tx0, yb - ty0, bgb)
+                                        : window_value(j, stack, xb, yb, f, bgb);
                         if (j.bleach != IMFCS_BLEACH_NONE && bpb[11] != 0.f)
                             vb = bleach_correct(vb, bleach_f(bpb, j.bleach, j.poly_order, t, bs), bpb[9], bpb[10]);
                         vb -= bpb[12];

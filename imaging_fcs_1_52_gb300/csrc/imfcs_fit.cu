@@ -26,6 +26,9 @@ constexpr int kMaxPts = 160;
 cudaError_t launch_lm_k3(const FitArgs &a, bool big, int blocks, int threads, size_t smem, cudaStream_t s);
 cudaError_t launch_lm_k5(const FitArgs &a, bool big, int blocks, int threads, size_t smem, cudaStream_t s);
 cudaError_t launch_lm_k11(const FitArgs &a, bool big, int blocks, int threads, size_t smem, cudaStream_t s);
+// specialised kernel of the default fit (imfcs_lm_tirf.cu)
+bool lm_tirf_applies(const FitArgs &a, bool tirf_zero_held);
+cudaError_t launch_lm_tirf(const FitArgs &a, int blocks, int threads, cudaStream_t s);
 
 size_t lm_smem_bytes(const FitArgs &a, int km, int warps)
 {
@@ -48,6 +51,7 @@ cudaError_t launch_lm(const FitArgs &a, int num_sms, cudaStream_t stream)
         const cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), stream);
         if (e != cudaSuccess) return e;
     }
+    if (lm_tirf_applies(a, a.tirf_zero_held != 0)) return launch_lm_tirf(a, blocks, warps * 32, stream);
     if (km == 3) return launch_lm_k3(a, big, blocks, warps * 32, smem, stream);
     if (km == 5) return launch_lm_k5(a, big, blocks, warps * 32, smem, stream);
     return launch_lm_k11(a, big, blocks, warps * 32, smem, stream);

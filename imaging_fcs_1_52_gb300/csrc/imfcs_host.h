@@ -42,6 +42,9 @@ cudaError_t launch_stream(const Job &j, const void *stack, const float *bparams,
 cudaError_t launch_monitor_finalize(const Job &j, const LagInfo *li_dev, const float *bparams, int nseg,
                                     const float2 *segtot, const float2 *snap_part, const int *segbad,
                                     const int *snap_bad, float4 *mon, float4 *blkmon, cudaStream_t s);
+// N&B mode: lag-1 mean and covariance only (sum: npix doubles of scratch)
+cudaError_t launch_nb_lag1(const Job &j, const float *s0, const float4 *mon, double *sum, double *nb_mean,
+                           double *nb_cov, cudaStream_t s);
 cudaError_t launch_block(const Job &j, const float *s0, const float4 *blkmon, int nbseg, float *s1, float *s2,
                          float *segsum, int *ind, int *ok, cudaStream_t s);
 cudaError_t launch_binning(const float *in, float *out, int win, int hin, int wt, int ht,

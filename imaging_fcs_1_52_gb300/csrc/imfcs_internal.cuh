@@ -41,6 +41,11 @@ struct Job {
     int binx, biny, pixbinx, pixbiny;
     int cfx, cfy;
     int background;
+    // per-pixel background image (java:9671-9673, 9842-9845): per-trace sums
+    // of the rounded image over the trace's window for its values, and over
+    // the direct window for its averaged trace; nullptr = scalar background
+    const int *bg_trace;
+    const int *bg_avg;
     int is_ccf;
     int npix, ntrace;
     // correlator structure
@@ -92,8 +97,21 @@ __device__ __forceinline__ double ff_val(const ff &a) { return (double)a.hi + (d
 // ---------------------------------------------------------------------------
 // Window value of one trace at frame t (0-based, relative to job.first).
 // ---------------------------------------------------------------------------
+// Background subtracted from trace `trace`'s window sum (its values), and
+// from the window sums of its averaged trace.
+__device__ __forceinline__ int trace_bg(const Job &j, int trace)
+{
+    return j.bg_trace ? __ldg(&j.bg_trace[trace]) : j.background * j.binx * j.biny;
+}
+__device__ __forceinline__ int trace_bg_avg(const Job &j, int trace)
+{
+    return j.bg_avg ? __ldg(&j.bg_avg[trace]) : j.background * j.binx * j.biny;
+}
+
+// bg: the window's background sum (uint16 input; the float input arrives
+// background-subtracted).
 __device__ __forceinline__ float window_value(const Job &j, const void *stack, int x0, int y0,
-                                              int t)
+                                              int t, int bg)
 {
     const size_t fsz = (size_t)j.in_w * j.in_h;
     const size_t base = (size_t)(j.first + t) * fsz;
@@ -103,7 +121,7 @@ __device__ __forceinline__ float window_value(const Job &j, const void *stack, i
         for (int k = 0; k < j.biny; k++)
             for (int i = 0; i < j.binx; i++)
                 acc += (int)__ldg(&s[(size_t)(y0 + k) * j.in_w + x0 + i]);
-        return (float)(acc - j.background * j.binx * j.biny);
+        return (float)(acc - bg);
     } else {
         const float *s = (const float *)stack + base;
         float acc = 0.f;
@@ -113,51 +131,28 @@ __device__ __forceinline__ float window_value(const Job &j, const void *stack, i
     }
 }
 
-// Integer window sum (uint16 input) used by the averaged trace, which the
-// Java code accumulates in int (java:9839-9852).
-__device__ __forceinline__ int window_value_int(const Job &j, const void *stack, int x0, int y0,
-                                                int t)
-{
-    const size_t fsz = (size_t)j.in_w * j.in_h;
-    const size_t base = (size_t)(j.first + t) * fsz;
-    if (!j.input_float) {
-        const uint16_t *s = (const uint16_t *)stack + base;
-        int acc = 0;
-        for (int k = 0; k < j.biny; k++)
-            for (int i = 0; i < j.binx; i++)
-                acc += (int)__ldg(&s[(size_t)(y0 + k) * j.in_w + x0 + i]);
-        return acc - j.background * j.binx * j.biny;
-    } else {
-        const float *s = (const float *)stack + base;
-        float acc = 0.f;
-        for (int k = 0; k < j.biny; k++)
-            for (int i = 0; i < j.binx; i++) acc += __ldg(&s[(size_t)(y0 + k) * j.in_w + x0 + i]);
-        return (int)acc;
-    }
-}
-
 // N consecutive frames t..t+N-1 of one window (frames >= tmax read as 0).
 // The loads are issued back to back so that a thread keeps N requests in
 // flight (the streaming passes are latency-bound otherwise).
 template <int N>
 __device__ __forceinline__ void window_values(const Job &j, const void *stack, int x0, int y0, int t,
-                                              int tmax, float *v)
+                                              int tmax, int bg, float *v)
 {
     const size_t fsz = (size_t)j.in_w * j.in_h;
     if (!j.input_float && j.binx == 1 && j.biny == 1) {
         const uint16_t *s = (const uint16_t *)stack + (size_t)j.first * fsz + (size_t)y0 * j.in_w + x0;
         unsigned short r[N];
 #pragma unroll
-        for (int u = 0; u < N; u++) r[u] = (t + u < tmax) ? __ldg(&s[(size_t)(t + u) * fsz]) : (unsigned short)j.background;
+        for (int u = 0; u < N; u++) r[u] = (t + u < tmax) ? __ldg(&s[(size_t)(t + u) * fsz]) : (unsigned short)0;
 #pragma unroll
-        for (int u = 0; u < N; u++) v[u] = (float)((int)r[u] - j.background);
+        for (int u = 0; u < N; u++) v[u] = (t + u < tmax) ? (float)((int)r[u] - bg) : 0.f;
     } else {
 #pragma unroll
-        for (int u = 0; u < N; u++) v[u] = (t + u < tmax) ? window_value(j, stack, x0, y0, t + u) : 0.f;
+        for (int u = 0; u < N; u++) v[u] = (t + u < tmax) ? window_value(j, stack, x0, y0, t + u, bg) : 0.f;
     }
 }
 
-__device__ __forceinline__ void trace_origin(const Job &j, int trace, int &x0, int &y0)
+__host__ __device__ __forceinline__ void trace_origin(const Job &j, int trace, int &x0, int &y0)
 {
     int pix = trace < j.npix ? trace : trace - j.npix;
     int ox = pix % j.out_w, oy = pix / j.out_w;

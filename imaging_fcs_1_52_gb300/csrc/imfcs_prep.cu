@@ -28,6 +28,7 @@ __global__ void __launch_bounds__(256) trace_kernel(Job j, const void *stack, fl
     int x0 = 0, y0 = 0;
     const bool valid = trace < j.ntrace;
     if (valid) trace_origin(j, trace, x0, y0);
+    const int bg = valid ? trace_bg_avg(j, trace) : 0;
     for (int r = 0; r < 4; r++) {
         int xl = ty * 4 + r, x = xbase + xl;
         float val = 0.f;
@@ -36,7 +37,7 @@ __global__ void __launch_bounds__(256) trace_kernel(Job j, const void *stack, fl
             const int fb = x * j.ave, fe = (x + 1) * j.ave;
             for (int f = fb; f < fe; f += 8) {
                 float v[8];
-                window_values<8>(j, stack, x0, y0, f, fe, v);
+                window_values<8>(j, stack, x0, y0, f, fe, bg, v);
 #pragma unroll
                 for (int u = 0; u < 8; u++) sum += (int)v[u];
             }
@@ -377,6 +378,63 @@ __device__ __noinline__ double exp_normal(const float *y, int n, float dts, floa
     return warp_sum_d(c2d);
 }
 
+// FP32 evaluation for phase 1 (no FP64 operation: GB300 issues FP64 at 1/64
+// of the FP32 rate): chi^2, A = J^T J, g = J^T r at the FP32 parameters.
+template <int K>
+__device__ __noinline__ float exp_normal32(const float *y, int n, float dts, float iy, const float *pf, float *A,
+                                           float *g, int lane)
+{
+    constexpr int NC = (K - 1) / 2;
+    constexpr int NA = K * (K + 1) / 2;
+    float acc[NA], gf[K], ik[NC];
+    for (int i = 0; i < NA; i++) acc[i] = 0.f;
+    for (int i = 0; i < K; i++) gf[i] = 0.f;
+    for (int c = 0; c < NC; c++) ik[c] = 1.f / pf[2 + 2 * c];
+    float c2f = 0.f;
+    for (int x = lane; x < n; x += 32) {
+        const float t = ((float)x + 0.5f) * dts;
+        float gr[K];
+        gr[0] = 1.f;
+        float f = pf[0];
+        for (int c = 0; c < NC; c++) {
+            float u, du;
+            exp_u_f(pf[2 + 2 * c], ik[c], t, u, du);
+            f -= pf[1 + 2 * c] * u;
+            gr[1 + 2 * c] = -u;
+            gr[2 + 2 * c] = -pf[1 + 2 * c] * du;
+        }
+        const float r = __ldg(&y[x]) * iy - f;
+        c2f = fmaf(r, r, c2f);
+        int qa = 0;
+        for (int a = 0; a < K; a++)
+            for (int b = 0; b <= a; b++) acc[qa++] += gr[a] * gr[b];
+        for (int a = 0; a < K; a++) gf[a] += gr[a] * r;
+    }
+    int qa = 0;
+    for (int a = 0; a < K; a++)
+        for (int b = 0; b <= a; b++) {
+            const float v = warp_sum(acc[qa++]);
+            A[a * K + b] = v;
+            A[b * K + a] = v;
+        }
+    for (int a = 0; a < K; a++) g[a] = warp_sum(gf[a]);
+    return warp_sum(c2f);
+}
+
+// FP32 counterpart of exp_newton_step (phase 1).
+template <int K>
+__device__ __forceinline__ bool exp_newton_step32(const float *A, const float *g, const float *p, unsigned &fix,
+                                                  float *h)
+{
+    constexpr int NC = (K - 1) / 2;
+    fix = 0;
+    bool ok = solve_scaled_k<K>(A, g, 0.f, 0u, h);
+    for (int c = 0; c < NC; c++)
+        if (p[2 + 2 * c] <= 0.f && (!ok || h[2 + 2 * c] < 0.f)) fix |= 1u << (2 + 2 * c);
+    if (fix) ok = solve_scaled_k<K>(A, g, 0.f, fix, h);
+    return ok;
+}
+
 // The undamped (Gauss-)Newton step on A h = g, with a rate at its bound
 // k = 0 held there (bit set in `fix`) when its step points below it.  The
 // rate form is continuous through k = 0 (tau = infinity), so a trace whose
@@ -427,30 +485,57 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         float syy = 0.f;
         for (int x = lane; x < n; x += 32) { const float yc = __ldg(&y[x]) * iy - my; syy = fmaf(yc, yc, syy); }
         syy = warp_sum(syy);
+        // eight rates per pass over the trace: independent recurrences and
+        // reductions overlap (the per-rate sums are those of one rate at a
+        // time, so the choice is the same)
+        constexpr int RB = 8;
         float bc = 3.4e38f, b0 = 0.f, b1 = 0.f, bk = 0.f;
-        for (int jg = 0; jg < 97; jg++) {
-            const float kx = jg == 0 ? 0.f : exp10f(-3.f + 7.f * (float)(jg - 1) / 95.f);
-            const float q = __expf(-kx * 32.f * dts);
-            const float e0 = __expf(-kx * ((float)lane + 0.5f) * dts);
-            float se = 0.f, e = e0;
-            for (int x = lane; x < n; x += 32) {
-                se += jg == 0 ? ((float)x + 0.5f) * dts : e;
-                e *= q;
+        for (int jb = 0; jb < 97; jb += RB) {
+            float kx[RB], q[RB], e0[RB], se[RB], e[RB];
+#pragma unroll
+            for (int r = 0; r < RB; r++) {
+                const int jg = jb + r;
+                kx[r] = (jg == 0 || jg > 96) ? 0.f : exp10f(-3.f + 7.f * (float)(jg - 1) / 95.f);
+                q[r] = __expf(-kx[r] * 32.f * dts);
+                e0[r] = __expf(-kx[r] * ((float)lane + 0.5f) * dts);
+                se[r] = 0.f;
+                e[r] = e0[r];
             }
-            const float me = warp_sum(se) / (float)n;
-            float see = 0.f, sye = 0.f;
-            e = e0;
             for (int x = lane; x < n; x += 32) {
-                const float b = (jg == 0 ? ((float)x + 0.5f) * dts : e) - me;
-                see = fmaf(b, b, see);
-                sye = fmaf(__ldg(&y[x]) * iy - my, b, sye);
-                e *= q;
+                const float tt = ((float)x + 0.5f) * dts;
+#pragma unroll
+                for (int r = 0; r < RB; r++) {
+                    se[r] += (jb + r == 0) ? tt : e[r];
+                    e[r] *= q[r];
+                }
             }
-            see = warp_sum(see);
-            sye = warp_sum(sye);
-            const float c1 = see > 0.f ? sye / see : 0.f;
-            const float c2 = syy - c1 * sye;
-            if (c2 < bc) { bc = c2; b1 = c1; b0 = my - c1 * me; bk = kx; }
+            float me[RB], see[RB], sye[RB];
+#pragma unroll
+            for (int r = 0; r < RB; r++) {
+                me[r] = warp_sum(se[r]) / (float)n;
+                see[r] = 0.f;
+                sye[r] = 0.f;
+                e[r] = e0[r];
+            }
+            for (int x = lane; x < n; x += 32) {
+                const float tt = ((float)x + 0.5f) * dts;
+                const float yc = __ldg(&y[x]) * iy - my;
+#pragma unroll
+                for (int r = 0; r < RB; r++) {
+                    const float b = ((jb + r == 0) ? tt : e[r]) - me[r];
+                    see[r] = fmaf(b, b, see[r]);
+                    sye[r] = fmaf(yc, b, sye[r]);
+                    e[r] *= q[r];
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < RB; r++) {
+                const float sE = warp_sum(see[r]), sY = warp_sum(sye[r]);
+                if (jb + r > 96) continue;
+                const float c1 = sE > 0.f ? sY / sE : 0.f;
+                const float c2 = syy - c1 * sY;
+                if (c2 < bc) { bc = c2; b1 = c1; b0 = my - c1 * me[r]; bk = kx[r]; }
+            }
         }
         if (bk == 0.f) { p[0] = b0; p[1] = -b1; p[2] = 0.0; }                  // f = c0 + c1 t
         else { p[0] = (double)b0 + b1; p[1] = (double)b1 * bk; p[2] = bk; }       // f = c0 + c1 e^{-kt}
@@ -463,49 +548,51 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
             p[0] = y1; p[1] = 0.5 * y1 / t10; p[2] = 1.0 / t10; p[3] = 0.5 * y1 / thalf; p[4] = 1.0 / thalf;
         }
     }
-    // Phase 1: FP32 Levenberg-Marquardt until the Gauss-Newton step is below
-    // 1e-4 sigma + 1e-6 |p| (or no step lowers chi^2 up to lambda 1e10).
+    // Phase 1: FP32 Levenberg-Marquardt (FP32 parameters, no FP64 operation)
+    // until the Gauss-Newton step is below 1e-4 sigma + 1e-6 |p| (or no step
+    // lowers chi^2 up to lambda 1e10).
     float A[K * K], lambda = 1e-3f;
     double g[K];
-    double chi2 = exp_normal<K>(y, n, dts, iy, p, false, A, g, lane);
-    const bool ok = isfinite(chi2);
+    float pf[K], gf[K];
+    for (int a = 0; a < K; a++) pf[a] = (float)p[a];
+    float chi2f = exp_normal32<K>(y, n, dts, iy, pf, A, gf, lane);
+    const bool ok = isfinite(chi2f);
     int evals = 1;
     for (int it_n = 0; ok && it_n < 100; it_n++) {
         float h[K];
         unsigned fix;
-        if (exp_newton_step<K>(A, g, p, fix, h)) {
+        if (exp_newton_step32<K>(A, gf, pf, fix, h)) {
             bool conv = true;
             for (int a = 0; a < K; a++) {
                 if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
-                conv = conv && fabsf(h[a]) <= 1e-6f * (float)fabs(p[a]) + 1e-4f * sig;
+                conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(pf[a]) + 1e-4f * sig;
             }
             if (conv) break;
         }
-        float gf[K];
-        for (int a = 0; a < K; a++) gf[a] = (float)g[a];
         if (!solve_scaled_k<K>(A, gf, lambda, fix, h)) {
             lambda *= 10.f;
             if (lambda > 1e10f) break;
             continue;
         }
-        double pn[K];
-        for (int a = 0; a < K; a++) pn[a] = p[a] + (double)h[a];
-        for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmax(pn[2 + 2 * c], 0.0);
-        float An[K * K];
-        double gn[K];
-        const double c2n = exp_normal<K>(y, n, dts, iy, pn, false, An, gn, lane);
+        float pn[K];
+        for (int a = 0; a < K; a++) pn[a] = pf[a] + h[a];
+        for (int c = 0; c < NC; c++) pn[2 + 2 * c] = fmaxf(pn[2 + 2 * c], 0.f);
+        float An[K * K], gn[K];
+        const float c2n = exp_normal32<K>(y, n, dts, iy, pn, An, gn, lane);
         evals++;
-        if (isfinite(c2n) && c2n < chi2) {
-            for (int a = 0; a < K; a++) { p[a] = pn[a]; g[a] = gn[a]; }
+        if (isfinite(c2n) && c2n < chi2f) {
+            for (int a = 0; a < K; a++) { pf[a] = pn[a]; gf[a] = gn[a]; }
             for (int a = 0; a < K * K; a++) A[a] = An[a];
-            chi2 = c2n;
+            chi2f = c2n;
             lambda = fmaxf(lambda * 0.1f, 1e-12f);
         } else {
             lambda *= 10.f;
             if (lambda > 1e10f) break;
         }
     }
+    for (int a = 0; a < K; a++) p[a] = (double)pf[a];
+    double chi2 = chi2f;
     // Phase 2: Newton with the full Hessian, float-float residuals and
     // gradient, to the least-squares minimum: until the step is below
     // 1e-9 sigma + 1e-12 |p|, while chi^2 does not increase.

@@ -205,6 +205,7 @@ float *plan_bparams(imfcs_plan *pl);
 const Job &plan_job(imfcs_plan *pl);
 void plan_umap(imfcs_plan *pl, double &uscale, double &uoff);
 const LagInfo &plan_laginfo(imfcs_plan *pl);
+void plan_set_nb_only(imfcs_plan *pl, bool on);
 }  // namespace imfcs
 
 extern "C" int imfcs_calc_acf(const float *pixels, double *pixels1, double *blockvararray,
@@ -261,8 +262,22 @@ extern "C" int imfcs_calc_acf(const float *pixels, double *pixels1, double *bloc
         CKR(cudaMemcpy(plan_bparams(pl), bp.data(), bp.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     o.acf = acf; o.var = var; o.nb_mean = nbm; o.nb_cov = nbc; o.blocked_ind = bind; o.blocked_ok = bok;
+    // N&B mode (agpufitjni.cu:5719-5720): lag 1 only; the ACF, variance and
+    // blocking outputs are left as the caller passed them (the reference
+    // copies back host arrays it never filled in this mode)
+    plan_set_nb_only(pl, p->isNBcalculation != 0);
     if (plan_execute_any(pl, din, &o, nullptr)) { rc = 1; goto cleanup; }
     CKR(cudaDeviceSynchronize());
+    if (p->isNBcalculation) {
+        if (NBmean) CKR(cudaMemcpy(NBmean, nbm, npix * sizeof(double), cudaMemcpyDeviceToHost));
+        if (NBcov) CKR(cudaMemcpy(NBcov, nbc, npix * sizeof(double), cudaMemcpyDeviceToHost));
+        const LagInfo &li = plan_laginfo(pl);
+        for (int x = 0; x < chanum; x++) {
+            if (lag) lag[x] = li.lag[x];
+            if (samp) samp[x] = (double)(1 << li.level[x]);
+        }
+        goto cleanup;
+    }
     h_acf.resize((size_t)npix * chanum);
     h_var.resize((size_t)npix * chanum);
     h_ind.resize(npix);

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __g
     const int pix = row * j.out_w + (valid ? ox : 0);
     const int xa = xoff + tid * j.pixbinx + (j.cfx < 0 ? -j.cfx : 0), ya = (j.cfy < 0 ? -j.cfy : 0);
     const int xb = xa + j.cfx, yb = ya + j.cfy;
-    const int bgsum = j.background * j.binx * j.biny;
+    const int bga = trace_bg(j, pix), bgb = CCF ? trace_bg(j, j.npix + pix) : 0;
     StreamCorr<MODE> ca, cb;
     ca.load(a.bparams + (size_t)pix * kBleachStride, j.frametime);
     if (CCF) cb.load(a.bparams + (size_t)(j.npix + pix) * kBleachStride, j.frametime);
@@ -219,11 +219,11 @@ __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __g
                         if (CCF) wb += (int)fb[f * a.bh * a.bw + k * a.bw + i];
                     }
                 const float va =
-                    ma.add(a, pix, t, ca.apply((float)(wa - bgsum), t, j.frametime, j.poly_order, a.basis));
+                    ma.add(a, pix, t, ca.apply((float)(wa - bga), t, j.frametime, j.poly_order, a.basis));
                 a.s0a[(size_t)t * j.npix + pix] = va;
                 if (CCF) {
                     const float vb = mb.add(a, j.npix + pix, t,
-                                            cb.apply((float)(wb - bgsum), t, j.frametime, j.poly_order, a.basis));
+                                            cb.apply((float)(wb - bgb), t, j.frametime, j.poly_order, a.basis));
                     a.s0b[(size_t)t * j.npix + pix] = vb;
                 }
             }
@@ -259,10 +259,11 @@ __global__ void __launch_bounds__(128) stream_plain_kernel(StreamArgs a)
         MonAcc m;
         m.init(a, t0);
         float *dst = tr ? a.s0b : a.s0a;
+        const int bg = trace_bg(j, trace);
         for (int tb = t0; tb < t1; tb += 8) {
             if (((tb - t0) & (kStF - 1)) == 0) c.seed(tb, j.frametime);
             float v[8];
-            window_values<8>(j, a.stack, x0, y0, tb, t1, v);
+            window_values<8>(j, a.stack, x0, y0, tb, t1, bg, v);
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int t = tb + u;
@@ -369,6 +370,50 @@ cudaError_t launch_stream(const Job &j, const void *stack, const float *bparams,
     default:
         return j.is_ccf ? launch_stream_t<0, true>(a, sp, mp, s) : launch_stream_t<0, false>(a, sp, mp, s);
     }
+}
+
+// ---------------------------------------------------------------------------
+// N&B mode (isNBcalculation, agpufitjni.cu:5719-5720 and calcacf2b
+// 5167-5180): only lag 1 is evaluated.  NBmean = the mean of the direct
+// window's first num-1 samples, NBcov = <I(t) I'(t+1)> - NBmean <I'>, over
+// the same num-1 products -- from the corrected, centred level-0 stream
+// (shift-invariant) and the lag-1 monitors.  Grid (pixel blocks, frame
+// segments); float-float segment sums combined by FP64 atomics.
+// ---------------------------------------------------------------------------
+constexpr int kNbSeg = 2048;
+
+__global__ void nb_lag1_kernel(int npix, int num, const float *s0a, const float *s0b, double *sum)
+{
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    const int t0 = blockIdx.y * kNbSeg, t1 = min(t0 + kNbSeg, num - 1);
+    ff acc = {0.f, 0.f};
+    for (int t = t0; t < t1; t++)
+        ff_add(acc, __ldg(&s0a[(size_t)t * npix + pix]) * __ldg(&s0b[(size_t)(t + 1) * npix + pix]));
+    atomicAdd(&sum[pix], ff_val(acc));
+}
+
+__global__ void nb_finalize_kernel(int npix, int chanum, int num, const float4 *mon, const double *sum,
+                                   double *nb_mean, double *nb_cov)
+{
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    const float4 m = mon[(size_t)pix * chanum + 1];   // (a, b, dm, Dm) of lag 1
+    const double n = (double)(num - 1);
+    if (nb_mean) nb_mean[pix] = m.z;
+    if (nb_cov) nb_cov[pix] = sum[pix] / n - (double)m.x * (double)m.y;
+}
+
+cudaError_t launch_nb_lag1(const Job &j, const float *s0, const float4 *mon, double *sum, double *nb_mean,
+                           double *nb_cov, cudaStream_t s)
+{
+    const float *s0a = s0, *s0b = j.is_ccf ? s0 + (size_t)j.npix * j.num : s0;
+    cudaError_t e = cudaMemsetAsync(sum, 0, sizeof(double) * j.npix, s);
+    if (e != cudaSuccess) return e;
+    dim3 grid((j.npix + 127) / 128, (j.num - 1 + kNbSeg - 1) / kNbSeg);
+    nb_lag1_kernel<<<grid, 128, 0, s>>>(j.npix, j.num, s0a, s0b, sum);
+    nb_finalize_kernel<<<(j.npix + 127) / 128, 128, 0, s>>>(j.npix, j.chanum, j.num, mon, sum, nb_mean, nb_cov);
+    return cudaGetLastError();
 }
 
 }  // namespace imfcs

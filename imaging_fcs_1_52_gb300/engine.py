@@ -195,6 +195,19 @@ class Plan:
             raise _lib.ImfcsError(_lib.last_error())
         return out
 
+    def set_background_image(self, bg):
+        """Per-pixel background (imfcs_plan_set_background_image): bg
+        [height][width] of the input frames, the mean background of each raw
+        pixel (rounded per pixel as the plugin does); None = the scalar one."""
+        if bg is None:
+            check(self._L.imfcs_plan_set_background_image(self._h, None), "imfcs_plan_set_background_image")
+            return
+        a = np.ascontiguousarray(bg, np.float64)
+        if a.shape != (self.cfg.height, self.cfg.width):
+            raise ValueError(f"background image must be {self.cfg.height} x {self.cfg.width}")
+        check(self._L.imfcs_plan_set_background_image(self._h, C.c_void_p(a.ctypes.data)),
+              "imfcs_plan_set_background_image")
+
     def set_surrogate(self, surrogate, mode: int = 1):
         """Seed the do_fit LM from a trained surrogate (imfcs_plan_set_surrogate):
         mode 1 refits failed seeded fits from the configured initial values;

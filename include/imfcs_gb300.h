@@ -348,6 +348,17 @@ IMFCS_API int imfcs_surrogate_predict(imfcs_surrogate *s, const float *dev_x, in
  *         judge of the seeded one).
  * The plan keeps the pointer; the surrogate must outlive its use. */
 IMFCS_API int imfcs_plan_set_surrogate(imfcs_plan *plan, imfcs_surrogate *s, int mode);
+/* Per-pixel background image, the plugin's background-file mode (bgrloaded:
+ * getIntensity java:9671-9673, calcIntensityTrace java:9842-9845).
+ * host_bg[height][width] in the input frame's geometry holds each raw
+ * pixel's mean background; its value rounded as Math.round does replaces the
+ * scalar background of that pixel.  As in the reference, the averaged
+ * intensity traces (the bleach fits' input) of a cross-correlation's second
+ * window subtract the background of the first window's pixels.  NULL
+ * restores the scalar background.  uint16 plans only (the float-stack
+ * calcACF path receives background-subtracted data, java:14959-14983). */
+IMFCS_API int imfcs_plan_set_background_image(imfcs_plan *plan, const double *host_bg);
+
 /* After an execute with a surrogate attached (synchronise first): pixels
  * refit from the configured initial values, and (mode 2) pixels whose
  * seeded chi^2 exceeded the plain chi^2 by more than 1 %. */

@@ -72,8 +72,8 @@ def _declare(L):
     L.imfcs_o_get_intensity.argtypes = [_u16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, _dp]
     L.imfcs_o_intensity_trace.argtypes = [_u16p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
-                                          C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                                          C.c_int, C.c_double, _dp, _dp]
+                                          C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.c_void_p, C.c_int, C.c_double, _dp, _dp]
     L.imfcs_o_poly_fit.argtypes = [_dp, _dp, C.c_int, C.c_int, _dp]
     L.imfcs_o_exp_fit.argtypes = [_dp, _dp, C.c_int, _dp]
     L.imfcs_o_dexp_fit.argtypes = [_dp, _dp, C.c_int, _dp]
@@ -130,7 +130,9 @@ def get_intensity(stack, px, py, binx=1, biny=1, bckg=0, first=0, num=None, bgr=
 
 
 def intensity_trace(stack, px, py, binx=1, biny=1, bckg=0, frametime=1e-3, first=0, num=None,
-                    bgr=None):
+                    bgr=None, bg_window=None):
+    """Averaged trace of the window at (px, py); bg_window = (x, y) of the
+    window whose background-image values are subtracted (default: its own)."""
     stack = np.ascontiguousarray(stack, np.uint16)
     t, h, w = stack.shape
     num = t - first if num is None else num
@@ -138,7 +140,8 @@ def intensity_trace(stack, px, py, binx=1, biny=1, bckg=0, frametime=1e-3, first
     tr = np.zeros(nopit)
     tt = np.zeros(nopit)
     bgr_p = None if bgr is None else np.ascontiguousarray(bgr, np.int32).ctypes.data
-    lib().imfcs_o_intensity_trace(stack, w, h, first, num, px, py, binx, biny, bckg, bgr_p, nopit,
+    bgx, bgy = (px, py) if bg_window is None else bg_window
+    lib().imfcs_o_intensity_trace(stack, w, h, first, num, px, py, bgx, bgy, binx, biny, bckg, bgr_p, nopit,
                                   frametime, tr, tt)
     return tr, tt
 

@@ -68,9 +68,14 @@ void imfcs_o_get_intensity(const uint16_t *stack, int width, int height, int fir
     }
 }
 
+/* bgx, bgy: the window whose background-image pixels are subtracted.  The
+ * reference subtracts the first (direct) window's values from both traces of
+ * a cross-correlation (bckg1 and bckg2 both read bgrmean[ipx1 + i][ipy1 + k],
+ * java:9842-9845); with a scalar background the two coincide. */
 void imfcs_o_intensity_trace(const uint16_t *stack, int width, int height, int first, int num,
-                             int px, int py, int binx, int biny, int bckg, const int *bgr,
-                             int nopit, double frametime, double *trace, double *trace_time)
+                             int px, int py, int bgx, int bgy, int binx, int biny, int bckg,
+                             const int *bgr, int nopit, double frametime, double *trace,
+                             double *trace_time)
 {
     size_t fsz = (size_t)width * height;
     int ave = (int)floor((double)num / nopit);
@@ -81,7 +86,7 @@ void imfcs_o_intensity_trace(const uint16_t *stack, int width, int height, int f
             for (int k = 0; k < biny; k++)
                 for (int y = first + x * ave; y <= first + (x + 1) * ave - 1; y++)
                     sum += (int)stack[(size_t)y * fsz + (size_t)(py + k) * width + px + i] -
-                           bg_at(bgr, width, px + i, py + k, bckg);
+                           bg_at(bgr, width, bgx + i, bgy + k, bckg);
         trace_time[x] = frametime * (x + 0.5) * ave;
         trace[x] = (double)(sum / ave);
     }
@@ -1081,6 +1086,7 @@ static void fcs_points(const double *p, double *f, double *jac, void *vctx)
 static int param_cov(const double *jw, int n, int k, const int *idx, double *cov, double *sigma)
 {
     double jtj[64 * 64], inv[64 * 64];
+    if (k < 1 || k > 64) return 1;
     for (int a = 0; a < k; a++)
         for (int b = 0; b < k; b++) {
             double s = 0.0;
@@ -1368,7 +1374,7 @@ int imfcs_o_run(const imfcs_o_config *cfg, const uint16_t *stack, const int *bgr
             imfcs_o_get_intensity(stack, cfg->width, cfg->height, cfg->first, num, px, py,
                                   cfg->binx, cfg->biny, cfg->background, bgr, c);
             if (cfg->bleach != IMFCS_O_BLEACH_NONE) {
-                imfcs_o_intensity_trace(stack, cfg->width, cfg->height, cfg->first, num, px, py,
+                imfcs_o_intensity_trace(stack, cfg->width, cfg->height, cfg->first, num, px, py, px1, py1,
                                         cfg->binx, cfg->biny, cfg->background, bgr, nopit,
                                         cfg->frametime, tr, tt);
                 int st = 0;

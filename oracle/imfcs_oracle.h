@@ -43,10 +43,12 @@ void imfcs_o_get_intensity(const uint16_t *stack, int width, int height, int fir
                            const int *bgr, double *out);
 
 /* calcIntensityTrace (Imaging_FCS_1_52.java:9822-9855): nopit averages with
- * Java int division; trace_time = frametime*(x+0.5)*ave. */
+ * Java int division; trace_time = frametime*(x+0.5)*ave.  The background
+ * image (bgr) is read at the window (bgx, bgy): the direct window for both
+ * traces of a cross-correlation, as java:9842-9845 does. */
 void imfcs_o_intensity_trace(const uint16_t *stack, int width, int height, int first,
-                             int num, int px, int py, int binx, int biny, int bckg,
-                             const int *bgr, int nopit, double frametime,
+                             int num, int px, int py, int bgx, int bgy, int binx, int biny,
+                             int bckg, const int *bgr, int nopit, double frametime,
                              double *trace, double *trace_time);
 
 /* Bleach fits on the averaged trace.  PolynomFit (java:10953-11004),

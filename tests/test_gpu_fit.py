@@ -390,3 +390,34 @@ def test_plan_spim_fit_on_a_stack(bright):
     both, errs = fit_errors(gpu, ref)
     assert both.sum() >= 48
     assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+
+
+def test_reference_calc_acf_nb_mode():
+    """N&B mode of calcACF (isNBcalculation, agpufitjni.cu:5719-5720): lag 1
+    only -- NBmean = mean of the first num-1 samples, NBcov = <I(t) I(t+1)>
+    minus the product of the two window means; the correlation outputs stay
+    as passed.  Equal to the full path's N&B outputs and to numpy."""
+    L = _lib.load()
+    raw = brownian_stack(7, 6, 3000, seed=17, density=2.0, cps=3e4)
+    pixels = np.ascontiguousarray(raw.astype(np.float32) - 100)
+    base = dict(width=7, height=6, win_star=7, hin_star=6, w_temp=7, h_temp=6, pixbinX=1, pixbinY=1,
+                binningX=1, binningY=1, firstframe=1, lastframe=3000, framediff=3000, cfXDistance=0,
+                cfYDistance=0, correlatorp=16, correlatorq=8, frametime=1e-3, background=100, chanum=73,
+                bleachcorr_gpu=0, bleachcorr_order=0, nopit=1000, ave=3)
+    out = {}
+    for nb in (0, 1):
+        p = _lib.ACFParameters(isNBcalculation=nb, **base)
+        acf = np.full(73 * 42, -7.0)
+        m, c = np.zeros(42), np.zeros(42)
+        rc = L.imfcs_calc_acf(pixels.ctypes.data, acf.ctypes.data, None, m.ctypes.data, c.ctypes.data, None, None,
+                              None, None, C.byref(p))
+        assert rc == 0, _lib.last_error()
+        out[nb] = (acf, m, c)
+    assert (out[1][0] == -7.0).all()                       # untouched in N&B mode
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=1e-6)
+    np.testing.assert_allclose(out[1][2], out[0][2], rtol=1e-5, atol=1e-6 * np.abs(out[0][2]).max())
+    x = pixels.reshape(3000, 42).astype(np.float64)
+    mean = x[:-1].mean(0)
+    cov = (x[:-1] * x[1:]).mean(0) - mean * x[1:].mean(0)
+    np.testing.assert_allclose(out[1][1], mean, rtol=1e-6)
+    np.testing.assert_allclose(out[1][2], cov, rtol=1e-4, atol=1e-5 * np.abs(cov).max())
