@@ -549,8 +549,10 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         }
     }
     // Phase 1: FP32 Levenberg-Marquardt (FP32 parameters, no FP64 operation)
-    // until the Gauss-Newton step is below 1e-4 sigma + 1e-6 |p| (or no step
-    // lowers chi^2 up to lambda 1e10).
+    // until the Gauss-Newton step is below 1e-3 sigma + 1e-6 |p| (or no step
+    // lowers chi^2 up to lambda 1e10): inside the region where the Newton
+    // phase converges quadratically; FP32 sums over 1000 points cannot
+    // resolve much smaller steps anyway.
     float A[K * K], lambda = 1e-3f;
     double g[K];
     float pf[K], gf[K];
@@ -566,7 +568,7 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
             for (int a = 0; a < K; a++) {
                 if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
-                conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(pf[a]) + 1e-4f * sig;
+                conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(pf[a]) + 1e-3f * sig;
             }
             if (conv) break;
         }

@@ -153,7 +153,7 @@ struct MonAcc {
 // next ones are in flight; a CTA barrier frees a box before thread 0 reloads
 // it.  The outcome of every bounded wait is made uniform across the CTA
 // (__syncthreads_or), so no thread is left waiting at a barrier.
-template <int MODE, bool CCF>
+template <int MODE, bool CCF, bool BIN1>
 __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     extern __shared__ __align__(128) unsigned char ssm[];
@@ -210,21 +210,40 @@ __global__ void __launch_bounds__(128) stream_tma_kernel(StreamArgs a, const __g
             const uint16_t *fa = tiles + (size_t)slot * box + ya * a.bw + xa;
             const uint16_t *fb = tiles + (size_t)slot * box + yb * a.bw + xb;
             const int n = min(kStF, t1 - tb);
-            for (int f = 0; f < n; f++) {
-                const int t = tb + f;
-                int wa = 0, wb = 0;
-                for (int k = 0; k < j.biny; k++)
-                    for (int i = 0; i < j.binx; i++) {
-                        wa += (int)fa[f * a.bh * a.bw + k * a.bw + i];
-                        if (CCF) wb += (int)fb[f * a.bh * a.bw + k * a.bw + i];
+            const int fstride = a.bh * a.bw;
+            float *da = a.s0a + (size_t)tb * j.npix + pix, *db = a.s0b + (size_t)tb * j.npix + pix;
+            if (BIN1 && n == kStF) {
+                // a full box of unbinned windows: one shared-memory load per
+                // frame and trace, the frame loop unrolled
+#pragma unroll 8
+                for (int f = 0; f < kStF; f++) {
+                    const int t = tb + f;
+                    const float va = ma.add(a, pix, t, ca.apply((float)((int)fa[f * fstride] - bga), t, j.frametime,
+                                                                j.poly_order, a.basis));
+                    da[(size_t)f * j.npix] = va;
+                    if (CCF) {
+                        const float vb = mb.add(a, j.npix + pix, t, cb.apply((float)((int)fb[f * fstride] - bgb), t,
+                                                                             j.frametime, j.poly_order, a.basis));
+                        db[(size_t)f * j.npix] = vb;
                     }
-                const float va =
-                    ma.add(a, pix, t, ca.apply((float)(wa - bga), t, j.frametime, j.poly_order, a.basis));
-                a.s0a[(size_t)t * j.npix + pix] = va;
-                if (CCF) {
-                    const float vb = mb.add(a, j.npix + pix, t,
-                                            cb.apply((float)(wb - bgb), t, j.frametime, j.poly_order, a.basis));
-                    a.s0b[(size_t)t * j.npix + pix] = vb;
+                }
+            } else {
+                for (int f = 0; f < n; f++) {
+                    const int t = tb + f;
+                    int wa = 0, wb = 0;
+                    for (int k = 0; k < j.biny; k++)
+                        for (int i = 0; i < j.binx; i++) {
+                            wa += (int)fa[f * fstride + k * a.bw + i];
+                            if (CCF) wb += (int)fb[f * fstride + k * a.bw + i];
+                        }
+                    const float va =
+                        ma.add(a, pix, t, ca.apply((float)(wa - bga), t, j.frametime, j.poly_order, a.basis));
+                    da[(size_t)f * j.npix] = va;
+                    if (CCF) {
+                        const float vb = mb.add(a, j.npix + pix, t,
+                                                cb.apply((float)(wb - bgb), t, j.frametime, j.poly_order, a.basis));
+                        db[(size_t)f * j.npix] = vb;
+                    }
                 }
             }
             if (tb + kStF >= min((seg + 1) * kSeg, t1)) {   // last box of the segment
@@ -311,7 +330,7 @@ static cudaError_t launch_stream_t(const StreamArgs &a, const StreamPlan &sp, co
 {
     const Job &j = a.j;
     if (map) {
-        auto kern = stream_tma_kernel<MODE, CCF>;
+        auto kern = (j.binx == 1 && j.biny == 1) ? stream_tma_kernel<MODE, CCF, true> : stream_tma_kernel<MODE, CCF, false>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.smem);
         if (e != cudaSuccess) return e;
         kern<<<dim3(sp.tiles_x * j.out_h, (a.nseg + kStSegs - 1) / kStSegs), 32 * sp.nw, sp.smem, s>>>(a, *map);
