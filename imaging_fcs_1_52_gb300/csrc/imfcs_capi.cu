@@ -265,8 +265,13 @@ struct imfcs_plan {
     int *bg_sums = nullptr;      // per-trace background sums [2][ntrace] (background image)
     bool nb_only = false;        // N&B mode of the reference calcACF: lag 1 only
     double *nb_sum = nullptr;    // its lag-1 product sums [npix]
-    // host path buffers
-    uint16_t *dstack = nullptr;
+    // host path buffers: the device stack (and, for the asynchronous host
+    // path, a second one: the copy of the next stack overlaps the current
+    // execution), the copy stream and the events ordering the two
+    uint16_t *dstack = nullptr, *dstack2 = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copied[2] = {}, consumed[2] = {};
+    int ring = 0;
     imfcs_outputs dout;
     bool dout_alloc = false;
     // stage timing
@@ -276,10 +281,16 @@ struct imfcs_plan {
     bool ev_used[kStages + 1] = {};
     ~imfcs_plan()
     {
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         for (auto &b : bufs) cudaFree(b.p);
         if (li_dev) cudaFree(li_dev);
         for (int i = 0; i <= kStages; i++)
             if (ev[i]) cudaEventDestroy(ev[i]);
+        for (int i = 0; i < 2; i++) {
+            if (copied[i]) cudaEventDestroy(copied[i]);
+            if (consumed[i]) cudaEventDestroy(consumed[i]);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
     }
     void mark(int i, cudaStream_t s)
     {
@@ -829,19 +840,29 @@ static cudaError_t d2h(T *host, const T *dev, size_t n, cudaStream_t s)
     return cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, s);
 }
 
-extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stack,
-                                       const imfcs_outputs *host_out, void *stream)
+// Enqueues one host-buffer execution on `s`: the stack copy on the plan's
+// copy stream into buffer `b` (after the execution that last read that
+// buffer), the execution after the copy, the results' copies after the
+// execution.  Returns without synchronising.
+static int execute_host_enqueue(imfcs_plan *pl, const uint16_t *host_stack, const imfcs_outputs *host_out,
+                                cudaStream_t s, int b)
 {
-    if (!pl || !host_stack || !host_out) { set_error("null argument"); return 1; }
-    cudaStream_t s = (cudaStream_t)stream;
     const imfcs_config &c = pl->cfg;
     const size_t np = pl->npix, ch = pl->chanum;
     const size_t fsz = (size_t)c.width * c.height;
-    if (!pl->dstack) {
+    uint16_t *&buf = b ? pl->dstack2 : pl->dstack;
+    if (!buf) {
         uint16_t *p = nullptr;
         cudaError_t e = pl->alloc(p, fsz * c.frames);
         if (e != cudaSuccess) { set_error(cuda_msg(e, "stack allocation")); return 1; }
-        pl->dstack = p;
+        buf = p;
+    }
+    if (!pl->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++) {
+            CK(cudaEventCreateWithFlags(&pl->copied[i], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&pl->consumed[i], cudaEventDisableTiming));
+        }
     }
     if (!pl->dout_alloc) {
         imfcs_outputs &d = pl->dout;
@@ -856,9 +877,13 @@ extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stac
         pl->dout_alloc = true;
     }
     // only the frames the job reads
-    CK(cudaMemcpyAsync(pl->dstack + fsz * c.first, host_stack + fsz * c.first, fsz * c.num * sizeof(uint16_t),
-                       cudaMemcpyHostToDevice, s));
-    if (imfcs_plan_execute(pl, pl->dstack, &pl->dout, stream)) return 1;
+    CK(cudaStreamWaitEvent(pl->copy_stream, pl->consumed[b], 0));
+    CK(cudaMemcpyAsync(buf + fsz * c.first, host_stack + fsz * c.first, fsz * c.num * sizeof(uint16_t),
+                       cudaMemcpyHostToDevice, pl->copy_stream));
+    CK(cudaEventRecord(pl->copied[b], pl->copy_stream));
+    CK(cudaStreamWaitEvent(s, pl->copied[b], 0));
+    if (imfcs_plan_execute(pl, buf, &pl->dout, s)) return 1;
+    CK(cudaEventRecord(pl->consumed[b], s));
     const imfcs_outputs &d = pl->dout;
     CK(d2h(host_out->acf, d.acf, np * ch, s));
     CK(d2h(host_out->var, d.var, np * ch, s));
@@ -873,11 +898,35 @@ extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stac
     CK(d2h(host_out->iterations, d.iterations, np, s));
     CK(d2h(host_out->bayes_prob, d.bayes_prob, np * 2, s));
     CK(d2h(host_out->covmats, d.covmats, np * (ch - 1) * (ch - 1), s));
+    return 0;
+}
+
+extern "C" int imfcs_plan_synchronize(imfcs_plan *pl, void *stream)
+{
+    if (!pl) { set_error("null plan"); return 1; }
+    cudaStream_t s = (cudaStream_t)stream;
     int derr = 0;
     CK(cudaMemcpyAsync(&derr, pl->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (derr) { set_error("a device-side wait timed out (TMA staging)"); return 1; }
     return 0;
+}
+
+extern "C" int imfcs_plan_execute_host(imfcs_plan *pl, const uint16_t *host_stack,
+                                       const imfcs_outputs *host_out, void *stream)
+{
+    if (!pl || !host_stack || !host_out) { set_error("null argument"); return 1; }
+    if (execute_host_enqueue(pl, host_stack, host_out, (cudaStream_t)stream, 0)) return 1;
+    return imfcs_plan_synchronize(pl, stream);
+}
+
+extern "C" int imfcs_plan_execute_host_async(imfcs_plan *pl, const uint16_t *host_stack,
+                                             const imfcs_outputs *host_out, void *stream)
+{
+    if (!pl || !host_stack || !host_out) { set_error("null argument"); return 1; }
+    const int b = pl->ring;
+    pl->ring ^= 1;
+    return execute_host_enqueue(pl, host_stack, host_out, (cudaStream_t)stream, b);
 }
 
 namespace imfcs {

@@ -258,6 +258,22 @@ class Plan:
               "imfcs_plan_execute_host")
         return outputs
 
+    def execute_host_async(self, stack: np.ndarray, outputs: dict, stream=None):
+        """Enqueue one host-buffer execution (imfcs_plan_execute_host_async):
+        the copy of the next stack overlaps this one's execution.  Use
+        page-locked arrays for stack and outputs; results are valid after
+        synchronize()."""
+        assert stack.flags["C_CONTIGUOUS"] and stack.dtype == np.uint16
+        self._async_keep = (stack, outputs)          # alive until synchronised
+        o = _outputs_struct({k: v.ctypes.data for k, v in outputs.items()})
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(self._L.imfcs_plan_execute_host_async(self._h, C.c_void_p(stack.ctypes.data), C.byref(o), sp),
+              "imfcs_plan_execute_host_async")
+
+    def synchronize(self, stream=None):
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(self._L.imfcs_plan_synchronize(self._h, sp), "imfcs_plan_synchronize")
+
 
 def run_host(stack: np.ndarray, cfg: FCSConfig) -> dict:
     plan = Plan(cfg)

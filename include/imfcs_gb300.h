@@ -262,6 +262,20 @@ IMFCS_API int imfcs_plan_execute(imfcs_plan *plan, const uint16_t *dev_stack, co
 IMFCS_API int imfcs_plan_execute_host(imfcs_plan *plan, const uint16_t *host_stack,
                             const imfcs_outputs *host_out, void *stream);
 
+/* Asynchronous form of imfcs_plan_execute_host for a sequence of stacks:
+ * enqueues the stack copy (on the plan's own copy stream, into one of two
+ * device stack buffers used in turn), the execution and the copies of the
+ * results on `stream`, and returns at once.  The copy of the next stack
+ * then overlaps the current execution.  With page-locked (pinned) host
+ * buffers the host thread does not wait; the host stack must stay unchanged
+ * until the execution that reads it has completed and the outputs are valid
+ * only after imfcs_plan_synchronize.  Successive calls on one plan write the
+ * same host output buffers unless the caller passes different ones. */
+IMFCS_API int imfcs_plan_execute_host_async(imfcs_plan *plan, const uint16_t *host_stack,
+                                  const imfcs_outputs *host_out, void *stream);
+/* Waits for the plan's executions on `stream`; reports a device-side error. */
+IMFCS_API int imfcs_plan_synchronize(imfcs_plan *plan, void *stream);
+
 /* FCS diffusion law (dlfit, java:11007-11231, determineDiffusionLaw 8190-8250,
  * fitDiffLaw 8253-8295): for binnings 1..n_bin the whole path is run on the
  * device-resident stack; out[3*n_bin] = {Aeff [um^2], mean D [um^2/s],
