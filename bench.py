@@ -11,8 +11,10 @@ stack (same generator, same seed).
 
 One step = the whole path over the full stack.  `value` is measured with the
 stack resident in HBM (1.64 GB, larger than L2, so no flush is needed);
-`e2e` goes through the C ABI with host buffers (imfcs_plan_execute_host:
-pinned host stack -> device, run, results -> host) every step.
+`e2e` goes through the C ABI with host buffers every step
+(imfcs_plan_execute_host_async: pinned host stack -> device on the plan's
+copy stream, run, results -> pinned host buffers; the next step's stack copy
+overlaps this step's run), synchronised once after the timed steps.
 
 --impl reference runs the reference's CPU implementation of the path: the
 Java CPU code cannot run here (no JVM), so the FP64 C restatement in oracle/
