@@ -33,7 +33,7 @@ EXPORTS = [
     "imfcs_surrogate_get_params", "imfcs_surrogate_set_params", "imfcs_surrogate_features",
     "imfcs_surrogate_gradients", "imfcs_surrogate_train", "imfcs_surrogate_predict",
     "imfcs_plan_set_surrogate", "imfcs_plan_surrogate_stats", "imfcs_plan_set_background_image",
-    "imfcs_plan_execute_host_async", "imfcs_plan_synchronize",
+    "imfcs_plan_execute_host_async", "imfcs_plan_synchronize", "imfcs_psf_calibration",
 ]
 
 
@@ -135,6 +135,7 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_plan_set_background_image.argtypes = [vp, vp]
     L.imfcs_plan_execute_host_async.argtypes = [vp, vp, C.POINTER(Outputs), vp]
     L.imfcs_plan_synchronize.argtypes = [vp, vp]
+    L.imfcs_psf_calibration.argtypes = [C.POINTER(Config), vp, C.c_int, C.c_int, dp, C.c_int, C.c_double, dp, vp]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

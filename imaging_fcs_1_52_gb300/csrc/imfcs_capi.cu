@@ -640,6 +640,8 @@ static int run_fit_seeded(imfcs_plan *pl, cudaStream_t s, const double *acf, con
 }
 
 namespace imfcs {
+int fit_stage(imfcs_plan *pl, cudaStream_t s, const double *acf, const double *var, const imfcs_outputs *dev_out);
+
 int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *dev_out, void *stream)
 {
     if (!pl || !dev_stack || !dev_out) { set_error("null argument"); return 1; }
@@ -701,6 +703,17 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
         pl->launches += 1;
     }
     pl->mark(5, s);
+    if (fit_stage(pl, s, acf, var, dev_out)) return 1;
+    pl->mark(6, s);
+    return 0;
+}
+
+// The fits over the correlator outputs acf/var of the plan's last execution
+// (with the plan's current model constants).
+int fit_stage(imfcs_plan *pl, cudaStream_t s, const double *acf, const double *var, const imfcs_outputs *dev_out)
+{
+    const imfcs_config &c = pl->cfg;
+    const int chanum = pl->chanum;
     if (c.do_fit || c.bayes) {
         const float *y = c.gls ? pl->ytrans : pl->fit_y;
         const float *w = c.gls ? nullptr : pl->fit_w;
@@ -733,7 +746,6 @@ int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs 
             }
         }
     }
-    pl->mark(6, s);
     return 0;
 }
 }  // namespace imfcs
@@ -1054,6 +1066,88 @@ extern "C" int imfcs_diffusion_law(const imfcs_config *cfg, const uint16_t *dev_
         line[0] = (sy - line[1] * sx) / sw;
     }
     return 0;
+}
+
+extern "C" int imfcs_psf_calibration(const imfcs_config *cfg, const uint16_t *dev_stack, int n_bin, int bin_start,
+                                     const double *psf_m, int psf_count, double pixel_size_m, double *out,
+                                     void *stream)
+{
+    if (!cfg || !dev_stack || !out || !psf_m || n_bin < 1) { set_error("invalid argument"); return 1; }
+    if (cfg->width < 20 || cfg->height < 20) {
+        set_error("Image is too small to provide good PSF statistics. At least 20x20 pixels are required.");
+        return 1;
+    }
+    if (psf_count < 1 || psf_count >= 10) {
+        set_error("PSF range and stepsize lead to too many calculations. Please chose a smaller range.");
+        return 1;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *acc = nullptr;
+    CK(cudaMalloc(&acc, 3 * sizeof(double)));
+    int rc = 0;
+    for (int u = n_bin; u >= 1 && rc == 0; u--) {
+        imfcs_config c = *cfg;
+        c.binx = c.biny = c.pixbinx = c.pixbiny = u;
+        c.map_x0 = c.map_y0 = 0;
+        c.out_w = c.width / u;
+        c.out_h = c.height / u;
+        c.cfx = c.cfy = 0;
+        c.do_fit = 1;
+        c.bayes = 0;
+        const double ax = pixel_size_m * u, ay = pixel_size_m * u;
+        c.cst[0] = ax; c.cst[1] = ay; c.cst[2] = psf_m[0]; c.cst[4] = 0; c.cst[5] = 0;
+        c.cst[6] = obsvol_2d_host(ax, ay, psf_m[0]);
+        imfcs_plan *pl = nullptr;
+        if (imfcs_plan_create(&c, &pl)) { rc = 1; break; }
+        const int np = pl->npix, ch = pl->chanum;
+        double *acf = nullptr, *var = nullptr;
+        float *fitres = nullptr, *chi2 = nullptr;
+        int *fitted = nullptr;
+        cudaError_t e = cudaMalloc(&acf, sizeof(double) * np * ch);
+        if (e == cudaSuccess) e = cudaMalloc(&var, sizeof(double) * np * ch);
+        if (e == cudaSuccess) e = cudaMalloc(&fitres, sizeof(float) * np * IMFCS_NPARAM);
+        if (e == cudaSuccess) e = cudaMalloc(&chi2, sizeof(float) * np);
+        if (e == cudaSuccess) e = cudaMalloc(&fitted, sizeof(int) * np);
+        if (e != cudaSuccess) { set_error(cuda_msg(e, "PSF calibration buffers")); rc = 1; }
+        imfcs_outputs o;
+        memset(&o, 0, sizeof(o));
+        o.acf = acf; o.var = var; o.fitres = fitres; o.chi2 = chi2; o.fitted = fitted;
+        // the correlations once per binning; the fits for every PSF size
+        if (!rc && imfcs_plan_execute(pl, dev_stack, &o, stream)) rc = 1;
+        for (int ip = 0; ip < psf_count && !rc; ip++) {
+            if (ip > 0) {
+                pl->cfg.cst[2] = psf_m[ip];
+                pl->cfg.cst[6] = obsvol_2d_host(ax, ay, psf_m[ip]);
+                if (fit_stage(pl, s, acf, var, &o)) { rc = 1; break; }
+            }
+            double h[3] = {0, 0, 0};
+            e = cudaMemsetAsync(acc, 0, 3 * sizeof(double), s);
+            if (e == cudaSuccess) {
+                dl_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(np, fitres, fitted, acc);
+                e = cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s);
+            }
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) { set_error(cuda_msg(e, "PSF calibration reduction")); rc = 1; break; }
+            // determinePSF (java:8141-8146): label u + psfBinStart for binning
+            // u + 1 (0-based u), mean D, and the variance of D over
+            // sqrt(width / (u + 1) * height / (u + 1)) in Java int arithmetic
+            const double meanD = h[1] * 1e12 / h[0];
+            const double varD = h[2] * 1e24 / h[0] - meanD * meanD;
+            const int ui = u - 1;
+            const int cnt = cfg->width / (ui + 1) * cfg->height / (ui + 1);
+            out[((size_t)ip * 3 + 0) * n_bin + ui] = ui + bin_start;
+            out[((size_t)ip * 3 + 1) * n_bin + ui] = meanD;
+            out[((size_t)ip * 3 + 2) * n_bin + ui] = varD / sqrt((double)cnt);
+        }
+        cudaFree(acf);
+        cudaFree(var);
+        cudaFree(fitres);
+        cudaFree(chi2);
+        cudaFree(fitted);
+        imfcs_plan_destroy(pl);
+    }
+    cudaFree(acc);
+    return rc;
 }
 
 extern "C" int imfcs_plan_bleach_params(const imfcs_plan *plan, float *host_out, int max_traces)

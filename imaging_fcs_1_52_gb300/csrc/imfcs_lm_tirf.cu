@@ -8,14 +8,17 @@
 // 11-parameter vector, so the parameters live in registers (no local-memory
 // arrays indexed at run time) and the executed code is a few kilobytes --
 // the generic kernel stalls on instruction fetch and local-memory loads.
+#include "imfcs_ff.cuh"
 #include "imfcs_lm.cuh"
 
 namespace imfcs {
 
 struct TirfC {
     float ax, ay, s2, inv_sz2, inv_norm;
-    double axd, ayd, sd, szd, inv_normd;
-    bool square;   // ax == ay: the two lateral factors coincide
+    double axd, ayd, sd, inv_sz2d, inv_normd;
+    f2 s2f, inv_normf;   // float-float copies for the precise residuals
+    bool square;         // ax == ay: the two lateral factors coincide
+    bool axial;          // the axial factor can differ from 1 in FP64 (finite sz)
 };
 
 // Lateral factor of a square-pixel window without offset or flow (the
@@ -29,8 +32,11 @@ __device__ __forceinline__ void tirf_lat(float a, float p0, float inv_p0, float 
     dL = 2.f * m * inv_sqrtpi;
 }
 
-// Model value and gradient (d/dN, d/dD; d/dG = 1) in FP32, internal units.
-__device__ __noinline__ float tirf_f(float N, float D, float G, const TirfC &c, float tau, float &gN, float &gD)
+// Model value and gradient (d/dN, d/dD; d/dG = 1) in FP32, internal units;
+// mag = |a/N| + |G|, the magnitude of the summed terms (the rounding error
+// of the value is relative to it).
+__device__ __noinline__ float tirf_f(float N, float D, float G, const TirfC &c, float tau, float &gN, float &gD,
+                                     float &mag)
 {
     const float p0 = sqrtf(fmaf(4.f * D, tau, c.s2));
     const float inv_p0 = 1.f / p0;
@@ -48,24 +54,92 @@ __device__ __noinline__ float tirf_f(float N, float D, float G, const TirfC &c, 
     const float iN = 1.f / N;
     gN = -a * iN * iN;
     gD = iN * da;
-    return __fmul_rn(a, iN) + G;
+    const float aN = __fmul_rn(a, iN);
+    mag = fabsf(aN) + fabsf(G);
+    return aN + G;
 }
 
-// FP64 model value (the precise residuals).
-__device__ __noinline__ double tirf_d(double N, double D, double G, const TirfC &c, double tau)
+// FP64 model value (the precise residuals), with as few FP64 divisions and
+// square roots as the accuracy allows (GB300 issues FP64 at 1/64 of the FP32
+// rate): 1/p0 from one reciprocal square root, 1/N once per evaluation
+// (inv_N), and the axial factor (1 + 4 D tau / sz^2)^(-1/2) only where it
+// differs from 1 in FP64 (a TIRF model's sz is ~1e6 um: 4 D tau / sz^2 <
+// 1e-17 and the factor rounds to exactly 1).
+__device__ __noinline__ double tirf_d(double inv_N, double D, double G, const TirfC &c, double tau)
 {
     const double inv_sqrtpi = 0.56418958354775628695;
-    const double p0 = sqrt(4.0 * D * tau + c.sd * c.sd);
-    double u = c.axd / p0;
+    const double p2 = 4.0 * D * tau + c.sd * c.sd;
+    const double ip0 = rsqrt(p2);
+    const double p0 = p2 * ip0;
+    double u = c.axd * ip0;
     const double lx = 2.0 * (p0 * inv_sqrtpi * expm1(-u * u) + c.axd * erf(u));
     double ly = lx;
     if (!c.square) {
-        u = c.ayd / p0;
+        u = c.ayd * ip0;
         ly = 2.0 * (p0 * inv_sqrtpi * expm1(-u * u) + c.ayd * erf(u));
     }
-    const double lat = lx * ly * c.inv_normd;
-    const double a1 = lat / sqrt(1.0 + 4.0 * D * tau / (c.szd * c.szd));
-    return a1 / N + G;
+    double a1 = lx * ly * c.inv_normd;
+    const double ax = 4.0 * D * tau * c.inv_sz2d;
+    if (ax > 1e-17) a1 *= rsqrt(1.0 + ax);
+    return a1 * inv_N + G;
+}
+
+// Float-float model value for the precise residuals: about 1e-12 relative,
+// far below what the residuals need (the data are FP32), on the FP32 pipes.
+// erf(u) = u sum_n e_n x^n with e_n = (2/sqrt(pi)) (-1)^n / (n! (2n+1)) and
+// expm1(-x) = -x sum_n q_n x^n with q_n = (-1)^n / (n+1)!, x = u^2, are the
+// Taylor series, truncated at n = 15: for u <= 1 the first omitted terms are
+// below 3e-14 and 5e-14.  Points with u > 1 (windows much wider than the
+// PSF) or an axial factor different from 1 in FP64 (SPIM) take the FP64
+// model instead.
+constexpr int kSeriesN = 16;
+__constant__ float kErfHi[kSeriesN], kErfLo[kSeriesN], kEm1Hi[kSeriesN], kEm1Lo[kSeriesN];
+
+__device__ __forceinline__ f2 ff_const(const float *hi, const float *lo, int n) { return {hi[n], lo[n]}; }
+
+// L = 2 (p0 / sqrt(pi) expm1(-u^2) + a erf(u)), u = a / p0 (float-float);
+// false when u > 1
+__device__ __forceinline__ bool tirf_lat_ff(float a, f2 p0, f2 ip0, f2 &L)
+{
+    const f2 u = f2_mul_f(ip0, a);
+    if (!(u.hi <= 1.f)) return false;
+    const f2 x = f2_mul(u, u);
+    f2 pe = ff_const(kErfHi, kErfLo, kSeriesN - 1), pq = ff_const(kEm1Hi, kEm1Lo, kSeriesN - 1);
+#pragma unroll
+    for (int n = kSeriesN - 2; n >= 0; n--) {
+        pe = f2_add(f2_mul(pe, x), ff_const(kErfHi, kErfLo, n));
+        pq = f2_add(f2_mul(pq, x), ff_const(kEm1Hi, kEm1Lo, n));
+    }
+    const f2 er = f2_mul(u, pe);                     // erf(u)
+    const f2 m = f2_neg(f2_mul(x, pq));               // expm1(-u^2)
+    const f2 inv_sqrtpi = {5.641896129e-01f, -2.931769139e-08f};   // 1/sqrt(pi) as float-float
+    const f2 t1 = f2_mul(f2_mul(p0, inv_sqrtpi), m);
+    const f2 t2 = f2_mul_f(er, a);
+    const f2 sum = f2_add(t1, t2);
+    L = {2.f * sum.hi, 2.f * sum.lo};
+    return true;
+}
+
+// Model value in float-float at (1/N, D, G); false where the FP64 model is
+// needed (see above).
+__device__ __forceinline__ bool tirf_value_ff(f2 inv_N, f2 D, f2 G, const TirfC &c, float tau, f2 &f)
+{
+    if (c.axial) return false;
+    // p0^2 = 4 D tau + s^2 (4 tau exact), 1/p0 by one Newton step on
+    // rsqrtf: e = 1 - p2 r^2, 1/p0 = r + r e / 2 (error ~e^2)
+    const f2 p2 = f2_add(f2_mul_f(D, 4.f * tau), c.s2f);
+    const float r = rsqrtf(p2.hi);
+    const f2 pr2 = f2_mul_f(f2_mul_f(p2, r), r);
+    const float e = (1.f - pr2.hi) - pr2.lo;
+    const f2 ip0 = f2_two_sum(r, 0.5f * r * e);
+    const f2 p0 = f2_mul(p2, ip0);
+    f2 Lx, Ly;
+    if (!tirf_lat_ff(c.ax, p0, ip0, Lx)) return false;
+    if (c.square) Ly = Lx;
+    else if (!tirf_lat_ff(c.ay, p0, ip0, Ly)) return false;
+    const f2 lat = f2_mul(f2_mul(Lx, Ly), c.inv_normf);
+    f = f2_add(f2_mul(lat, inv_N), G);
+    return true;
 }
 
 struct Tirf3 {
@@ -73,38 +147,30 @@ struct Tirf3 {
     float g[3];
     float chi2;      // FP32 phases
     double chi2d;    // FP64-residual evaluations
+    float fmag;      // sum w (|a/N| + |G|)^2: scale of the model values (FP32 phases)
 };
 
-// One evaluation over the fit's points (warp): chi^2, J^T W J, J^T W r, with
-// FP32 residuals, or (precise) residuals from the FP64 model value at the
-// double parameters (Nd, Dd, Gd).  The FP32 phases use no FP64 operation:
-// GB300 issues FP64 at 1/64 of the FP32 rate.
-__device__ __noinline__ void tirf_eval(const TirfC &c, float N, float D, float G, double Nd, double Dd, double Gd,
-                                       const float *yl, const float *wl, const float *xl, int n, int lane,
-                                       bool precise, Tirf3 &s)
+// One evaluation over the fit's points (warp): chi^2, J^T W J, J^T W r with
+// FP32 residuals.  No FP64 operation: GB300 issues FP64 at 1/64 of the FP32
+// rate, and the FP32 phases evaluate the model some twenty times per fit.
+__device__ __noinline__ void tirf_eval32(const TirfC &c, float N, float D, float G, const float *yl,
+                                         const float *wl, const float *xl, int n, int lane, Tirf3 &s)
 {
     float acc[9];
 #pragma unroll
     for (int i = 0; i < 9; i++) acc[i] = 0.f;
-    double c2acc = 0.0;
-    float c2f = 0.f;
+    float c2f = 0.f, fm = 0.f;
 #pragma unroll
     for (int m = 0; m < kPtsPerLane; m++) {
         const int i = lane + 32 * m;
         if (i < n) {
-            float gr[3];
+            float gr[3], mag;
             gr[2] = 1.f;
-            const float f = tirf_f(N, D, G, c, xl[m], gr[0], gr[1]);
+            const float f = tirf_f(N, D, G, c, xl[m], gr[0], gr[1], mag);
             const float w = wl[m];
-            float r;
-            if (precise) {
-                const double rd = (double)yl[m] - tirf_d(Nd, Dd, Gd, c, (double)xl[m]);
-                r = (float)rd;
-                c2acc += (double)w * rd * rd;
-            } else {
-                r = yl[m] - f;
-                c2f = fmaf(w * r, r, c2f);
-            }
+            const float r = yl[m] - f;
+            c2f = fmaf(w * r, r, c2f);
+            fm = fmaf(w * mag, mag, fm);
             int q = 0;
 #pragma unroll
             for (int p = 0; p < 3; p++)
@@ -125,16 +191,82 @@ __device__ __noinline__ void tirf_eval(const TirfC &c, float N, float D, float G
         }
 #pragma unroll
     for (int p = 0; p < 3; p++) s.g[p] = warp_sum(acc[q++]);
-    if (precise) {
-        s.chi2d = warp_sum_d(c2acc);
-        s.chi2 = (float)s.chi2d;
-    } else {
-        s.chi2 = warp_sum(c2f);
-        s.chi2d = 0.0;
+    s.chi2 = warp_sum(c2f);
+    s.chi2d = 0.0;
+    s.fmag = warp_sum(fm);
+}
+
+// The same with residuals of the model value in float-float at the FP64
+// parameters (Nd, Dd, Gd) -- FP64 model where the series do not apply --
+// the Jacobian in FP32 at their FP32 copies; chi^2 reduced in float-float.
+__device__ __noinline__ void tirf_eval64(const TirfC &c, double Nd, double Dd, double Gd, const float *yl,
+                                         const float *wl, const float *xl, int n, int lane, Tirf3 &s)
+{
+    const float N = (float)Nd, D = (float)Dd, G = (float)Gd;
+    const double inv_Nd = 1.0 / Nd;
+    const f2 inv_Nf = f2_from_d(inv_Nd), Df = f2_from_d(Dd), Gf = f2_from_d(Gd);
+    float acc[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) acc[i] = 0.f;
+    f2 c2acc = {0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < kPtsPerLane; m++) {
+        const int i = lane + 32 * m;
+        if (i < n) {
+            float gr[3], mag;
+            gr[2] = 1.f;
+            tirf_f(N, D, G, c, xl[m], gr[0], gr[1], mag);
+            const float w = wl[m];
+            f2 fv;
+            if (!tirf_value_ff(inv_Nf, Df, Gf, c, xl[m], fv))
+                fv = f2_from_d(tirf_d(inv_Nd, Dd, Gd, c, (double)xl[m]));
+            const f2 rr = f2_add(f2_from_f(yl[m]), f2_neg(fv));
+            const float r = f2_val(rr);
+            c2acc = f2_add(c2acc, f2_mul_f(f2_mul(rr, rr), w));
+            int q = 0;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int t = 0; t <= p; t++) acc[q++] += w * gr[p] * gr[t];
+#pragma unroll
+            for (int p = 0; p < 3; p++) acc[q++] += w * gr[p] * r;
+        }
     }
+    int q = 0;
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int t = 0; t <= p; t++) {
+            const float v = warp_sum(acc[q++]);
+            s.A[p * 3 + t] = v;
+            s.A[t * 3 + p] = v;
+        }
+#pragma unroll
+    for (int p = 0; p < 3; p++) s.g[p] = warp_sum(acc[q++]);
+    for (int o = 16; o > 0; o >>= 1) {
+        const f2 other = {__shfl_xor_sync(0xffffffffu, c2acc.hi, o), __shfl_xor_sync(0xffffffffu, c2acc.lo, o)};
+        c2acc = f2_add(c2acc, other);
+    }
+    s.chi2d = (double)c2acc.hi + (double)c2acc.lo;
+    s.chi2 = c2acc.hi + c2acc.lo;
+    s.fmag = 0.f;
+}
+
+// dispatch by phase
+__device__ __forceinline__ void tirf_eval(const TirfC &c, float N, float D, float G, double Nd, double Dd, double Gd,
+                                          const float *yl, const float *wl, const float *xl, int n, int lane,
+                                          bool precise, Tirf3 &s)
+{
+    if (precise) tirf_eval64(c, Nd, Dd, Gd, yl, wl, xl, n, lane, s);
+    else tirf_eval32(c, N, D, G, yl, wl, xl, n, lane, s);
 }
 
 __device__ __forceinline__ float tirf_sig(const Tirf3 &s, int i) { return rsqrtf(fmaxf(s.A[i * 3 + i], 1e-30f)); }
+
+// Bound on the relative rounding error of the FP32 model value (erff and
+// expm1f within a few ulp, ~15 roundings of the lateral, axial and final
+// terms): 4e-6, some 70 ulp.
+constexpr float kModelRound = 4e-6f;
 
 __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
 {
@@ -145,8 +277,14 @@ __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
     TirfC c;
     c.ax = a.mc.ax; c.ay = a.mc.ay; c.s2 = a.mc.s * a.mc.s; c.inv_sz2 = 1.f / (a.mc.sz * a.mc.sz);
     c.inv_norm = a.mc.inv_norm;
-    c.axd = a.mc.ax; c.ayd = a.mc.ay; c.sd = a.mc.s; c.szd = a.mc.sz; c.inv_normd = a.mc.inv_norm;
+    c.axd = a.mc.ax; c.ayd = a.mc.ay; c.sd = a.mc.s; c.inv_normd = a.mc.inv_norm;
+    c.inv_sz2d = 1.0 / ((double)a.mc.sz * (double)a.mc.sz);
     c.square = a.mc.ay == a.mc.ax;
+    c.s2f = f2_two_prod(a.mc.s, a.mc.s);
+    c.inv_normf = f2_from_f(a.mc.inv_norm);
+    // 4 D tau / sz^2 at the largest D and lag time a fit can reach is far
+    // below FP64 resolution for a TIRF sz; the axial factor is then exactly 1
+    c.axial = !(c.inv_sz2d * 4e6 < 1e-17);
     float xl[kPtsPerLane];
 #pragma unroll
     for (int m = 0; m < kPtsPerLane; m++) {
@@ -168,6 +306,7 @@ __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
         float pf[3] = {__ldg(&ip[0]), __ldg(&ip[1]), __ldg(&ip[4])};
         double pd[3] = {0.0, 0.0, 0.0};
         bool precise = false;     // parameters and chi^2 held in FP64 (pd, chi2d)
+        bool retried = false;     // Newton left its region once: FP32 LM to 1e-4 sigma, then Newton again
         Tirf3 s;
         tirf_eval(c, pf[0], pf[1], pf[2], 0.0, 0.0, 0.0, yl, wl, xl, n, lane, false, s);
         int state = IMFCS_STATE_MAX_ITERATIONS, it = 0, nprec = 0;
@@ -183,7 +322,7 @@ __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
 #pragma unroll
                     for (int i = 0; i < 3; i++) {
                         const float sig = tirf_sig(s, i);
-                        const float tol = precise ? 1e-7f * fabsf(pf[i]) + 1e-5f * sig : 1e-3f * sig;
+                        const float tol = precise ? 1e-7f * fabsf(pf[i]) + 1e-5f * sig : (retried ? 1e-4f : 1e-3f) * sig;
                         conv = conv && (fabsf(hg[i]) <= tol);
                     }
                     if (conv) {
@@ -253,10 +392,25 @@ __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
                         H[r * 3 + q] = v;
                         H[q * 3 + r] = v;
                     }
-                bool newton_done = false, left = false;
+                bool newton_done = false, left = false, stationary = false;
 #pragma unroll 1
                 for (int ni = 0; ni < 7 && !left; ni++) {
                     const bool fp64 = ni >= 3;
+                    if (fp64 && !precise && stationary) {
+                        // At the FP32 gradient's stationary point.  The FP32
+                        // model value's rounding error (below kModelRound of
+                        // the summed terms' magnitude, |a/N| + |G|) moves
+                        // the minimum by at most B sigma_i in parameter i,
+                        // B = kModelRound sqrt(sum w (|a/N| + |G|)^2)
+                        // (Cauchy-Schwarz in the metric of J^T W J).  Where
+                        // that is below 1e-5 of N and of D, the FP64 step
+                        // cannot matter at the 1e-4 parity bar: skip it.
+                        const float B = kModelRound * sqrtf(s.fmag);
+                        if (B * tirf_sig(s, 0) <= 1e-5f * fabsf(pf[0]) && B * tirf_sig(s, 1) <= 1e-5f * fabsf(pf[1])) {
+                            newton_done = true;
+                            break;
+                        }
+                    }
                     if (fp64) {
                         if (!precise) {
 #pragma unroll
@@ -283,11 +437,32 @@ __global__ void __launch_bounds__(128) lm_tirf_kernel(FitArgs a)
                     } else {
 #pragma unroll
                         for (int i = 0; i < 3; i++) pf[i] += hn[i];
-                        if (small) ni = 2;
-                        else tirf_eval(c, pf[0], pf[1], pf[2], 0.0, 0.0, 0.0, yl, wl, xl, n, lane, false, s);
+                        if (small) {
+                            ni = 2;
+                            stationary = true;
+                        } else {
+                            tirf_eval(c, pf[0], pf[1], pf[2], 0.0, 0.0, 0.0, yl, wl, xl, n, lane, false, s);
+                        }
                     }
                 }
                 if (newton_done) { state = IMFCS_STATE_CONVERGED; it++; break; }
+                if (!retried) {
+                    // Newton left its quadratic region (a step above 0.05
+                    // sigma) or met an indefinite Hessian: back to FP32 LM,
+                    // to the tighter 1e-4 sigma, and Newton from there -- an
+                    // LM on FP64-residual evaluations costs ~10x an FP32
+                    // iteration and runs for tens of iterations, and the few
+                    // fits that take it set the duration of the whole launch
+                    retried = true;
+                    if (precise) {
+#pragma unroll
+                        for (int i = 0; i < 3; i++) pf[i] = (float)pd[i];
+                        precise = false;
+                    }
+                    tirf_eval(c, pf[0], pf[1], pf[2], 0.0, 0.0, 0.0, yl, wl, xl, n, lane, false, s);
+                    lambda = 1e-3f;
+                    continue;
+                }
                 // otherwise LM on the FP64-residual model
                 if (!precise) {
 #pragma unroll
@@ -327,6 +502,25 @@ bool lm_tirf_applies(const FitArgs &a, bool tirf_zero_held)
 
 cudaError_t launch_lm_tirf(const FitArgs &a, int blocks, int threads, cudaStream_t s)
 {
+    // the series coefficients as float-float (hi = the float nearest the
+    // FP64 value, lo = the float nearest the remainder)
+    float eh[kSeriesN], el[kSeriesN], qh[kSeriesN], ql[kSeriesN];
+    const double two_sqrtpi = 1.1283791670955125739;   // 2 / sqrt(pi)
+    double fact = 1.0;                                 // n!
+    for (int n = 0; n < kSeriesN; n++) {
+        if (n > 0) fact *= n;
+        const double en = ((n & 1) ? -1.0 : 1.0) * two_sqrtpi / (fact * (2 * n + 1));
+        const double qn = ((n & 1) ? -1.0 : 1.0) / (fact * (n + 1));
+        eh[n] = (float)en;
+        el[n] = (float)(en - (double)eh[n]);
+        qh[n] = (float)qn;
+        ql[n] = (float)(qn - (double)qh[n]);
+    }
+    cudaError_t e = cudaMemcpyToSymbolAsync(kErfHi, eh, sizeof(eh), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kErfLo, el, sizeof(el), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kEm1Hi, qh, sizeof(qh), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kEm1Lo, ql, sizeof(ql), 0, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
     lm_tirf_kernel<<<blocks, threads, 0, s>>>(a);
     return cudaGetLastError();
 }

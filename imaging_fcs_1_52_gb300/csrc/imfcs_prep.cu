@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include "imfcs_internal.cuh"
+#include "imfcs_ff.cuh"
 #include "imfcs_host.h"
 
 namespace imfcs {
@@ -180,44 +181,6 @@ __device__ __forceinline__ float exp_dudk(float k, float ik, float t, float e, f
         return -t * t * d;
     }
     return (t * e - u) * ik;
-}
-
-// Float-float (double-single) arithmetic for the precise residuals: exact
-// two-sum / two-product (Knuth, Dekker) with explicitly rounded operations.
-struct f2 {
-    float hi, lo;
-};
-__device__ __forceinline__ f2 f2_quick(float a, float b)
-{
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ f2 f2_two_sum(float a, float b)
-{
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-__device__ __forceinline__ f2 f2_two_prod(float a, float b)
-{
-    const float p = __fmul_rn(a, b);
-    return {p, fmaf(a, b, -p)};
-}
-__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
-{
-    f2 s = f2_two_sum(a.hi, b.hi);
-    return f2_quick(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-}
-__device__ __forceinline__ f2 f2_neg(f2 a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
-{
-    f2 p = f2_two_prod(a.hi, b.hi);
-    return f2_quick(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
-}
-__device__ __forceinline__ f2 f2_from_d(double x)
-{
-    const float h = (float)x;
-    return {h, (float)(x - (double)h)};
 }
 
 // (A + lambda diag(A) + ridge) x = b on the Jacobi-scaled system, FP32;

@@ -287,6 +287,18 @@ IMFCS_API int imfcs_diffusion_law(const imfcs_config *cfg, const uint16_t *dev_s
                         int fit_lo, int fit_hi, double pixel_size_m, double psf_m,
                         double *out, double *line, void *stream);
 
+/* PSF calibration (determinePSF, java:8115-8160): for psf_count < 10 PSF
+ * sizes psf_m[i] (1/e^2 radius, m) and binnings 1..n_bin (the "All",
+ * non-overlap mode of dlfit), out[i][3][n_bin] receives what the plugin
+ * tabulates per binning: the label u + bin_start of binning u + 1, the mean
+ * fitted D [um^2/s] and the variance of D divided by
+ * sqrt(width / (u + 1) * height / (u + 1)) (Java int arithmetic).  The
+ * correlations are computed once per binning and fitted for every PSF.
+ * At least 20 x 20 pixels are required, as in the plugin. */
+IMFCS_API int imfcs_psf_calibration(const imfcs_config *cfg, const uint16_t *dev_stack, int n_bin, int bin_start,
+                          const double *psf_m, int psf_count, double pixel_size_m, double *out,
+                          void *stream);
+
 /* Seeded 2D Brownian-motion stack simulator (semantics of simulateACF2D,
  * java:13854-14409: Brownian steps, Gaussian PSF photon scatter, Poisson
  * emission, camera offset).  Writes dev_stack[frames][height][width].

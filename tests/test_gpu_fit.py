@@ -451,3 +451,42 @@ def test_async_host_path_matches_sync():
     for r, o in zip(ref, outs):
         for k in ("acf", "var", "blocked_ind", "fitres", "chi2", "fitted"):
             np.testing.assert_array_equal(o[k], r[k], err_msg=k)
+
+
+def test_psf_calibration():
+    """determinePSF (java:8115-8160): correlate once per binning, fit for
+    every PSF size; mean D and the tabulated spread per (PSF, binning) as the
+    oracle's fits give them."""
+    import torch
+    L = _lib.load()
+    raw = brownian_stack(20, 20, 3000, seed=43, density=2.0, cps=3e4)
+    dev = torch.from_numpy(raw.view(np.int16)).cuda().view(torch.uint16)
+    cfg = engine.FCSConfig(width=20, height=20, frames=3000, background=100)
+    c = cfg.to_c()
+    psfs = np.array([0.35e-6, 0.4e-6, 0.45e-6])
+    nbin, bin_start = 3, 2
+    out = np.zeros((3, 3, nbin))
+    rc = L.imfcs_psf_calibration(C.byref(c), C.c_void_p(dev.data_ptr()), nbin, bin_start,
+                                 psfs.ctypes.data_as(C.POINTER(C.c_double)), 3, C.c_double(0.24e-6),
+                                 out.ctypes.data_as(C.POINTER(C.c_double)), None)
+    assert rc == 0, _lib.last_error()
+    for ip, psf in enumerate(psfs):
+        for u in range(nbin):
+            b = u + 1
+            cst = engine.model_constants(binx=b, biny=b, psf_um=psf * 1e6)
+            r = oracle.run(raw, out_w=20 // b, out_h=20 // b, binx=b, biny=b, background=100,
+                           init=np.array(cfg.init), free_mask=np.array(cfg.free_mask, np.int32), cst=cst)
+            d = r["fitres"][r["fitted"] == 1, 1]
+            mean = d.mean() * 1e12
+            var = (d ** 2).mean() * 1e24 - mean ** 2
+            cnt = 20 // b * 20 // b                # Java int arithmetic, left to right
+            assert out[ip, 0, u] == u + bin_start
+            assert abs(out[ip, 1, u] - mean) <= 1e-4 * mean
+            assert abs(out[ip, 2, u] - var / np.sqrt(cnt)) <= 1e-3 * abs(var / np.sqrt(cnt)) + 1e-6
+    # the fitted D depends on the assumed PSF
+    assert out[0, 1, 0] != out[2, 1, 0]
+    c_small = engine.FCSConfig(width=19, height=20, frames=3000, background=100).to_c()
+    assert L.imfcs_psf_calibration(C.byref(c_small), C.c_void_p(dev.data_ptr()), 1, 1,
+                                   psfs.ctypes.data_as(C.POINTER(C.c_double)), 1, C.c_double(0.24e-6),
+                                   out.ctypes.data_as(C.POINTER(C.c_double)), None) != 0
+    assert "20x20" in _lib.last_error()
