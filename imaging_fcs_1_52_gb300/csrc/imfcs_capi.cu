@@ -47,7 +47,7 @@ bool build_lag_info(int p, int q, int num, LagInfo &li, int &chanum, int &blockn
                     std::string &err)
 {
     memset(&li, 0, sizeof(li));
-    if (p != kP) { err = "correlator P must be 16 in this build"; return false; }
+    if (p != 16 && p != 32) { err = "correlator P must be 16 or 32"; return false; }
     if (q < 2 || q > 8) { err = "correlator Q must be in 2..8 in this build"; return false; }
     chanum = (int)(p + (q - 1) * (double)p / 2 + 1);
     if (chanum > kMaxChan) { err = "too many correlation channels"; return false; }
@@ -283,6 +283,7 @@ struct imfcs_plan {
     {
         if (copy_stream) cudaStreamSynchronize(copy_stream);
         for (auto &b : bufs) cudaFree(b.p);
+        if (own_arena) cudaFree(own_arena);
         if (li_dev) cudaFree(li_dev);
         for (int i = 0; i <= kStages; i++)
             if (ev[i]) cudaEventDestroy(ev[i]);
@@ -297,6 +298,31 @@ struct imfcs_plan {
         if (!timing) return;
         cudaEventRecord(ev[i], s);
         ev_used[i] = true;
+    }
+    // per-execution scratch: one arena, owned by the plan or bound by a
+    // batch that runs several plans' executions one after another on it
+    struct ScratchField {
+        void **ptr;
+        size_t bytes;
+    };
+    std::vector<ScratchField> scratch;
+    size_t scratch_need = 0;
+    void *own_arena = nullptr;
+    template <class T>
+    void reserve(T *&ptr, size_t count)
+    {
+        size_t n = count * sizeof(T);
+        n = ((n ? n : 16) + 255) & ~(size_t)255;
+        scratch.push_back({reinterpret_cast<void **>(&ptr), n});
+        scratch_need += n;
+    }
+    void bind_scratch(void *base)
+    {
+        size_t off = 0;
+        for (auto &f : scratch) {
+            *f.ptr = base ? (void *)((char *)base + off) : nullptr;
+            off += f.bytes;
+        }
     }
     template <class T>
     cudaError_t alloc(T *&ptr, size_t count)
@@ -350,12 +376,18 @@ static bool validate_config(const imfcs_config *c, std::string &err)
         return false;
     }
     if (!(c->frametime > 0)) { err = "invalid frame time"; return false; }
+    // the GLS covariance and whitened fit hold the (chanum-1)^2 covariance
+    // and L^-1 of a pixel in one CTA's shared memory: P = 16 (chanum <= 97)
+    if (c->gls && c->p + (c->q - 1) * c->p / 2 > 96) {
+        err = "GLS needs at most 96 fit lags (correlator P = 16)";
+        return false;
+    }
     return true;
 }
 
 namespace imfcs {
 int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h, bool given_bleach,
-                   imfcs_plan **plan_out)
+                   imfcs_plan **plan_out, bool external_scratch)
 {
     std::string err;
     if (!plan_out) { set_error("null plan pointer"); return 1; }
@@ -407,27 +439,28 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
     cudaError_t e = cudaSuccess;
     const size_t nt = j.ntrace, np = j.npix;
 #define AL(ptr, n) if (e == cudaSuccess) e = pl->alloc(ptr, (size_t)(n))
+#define AS(ptr, n) pl->reserve(ptr, (size_t)(n))
     e = cudaMalloc(&pl->li_dev, sizeof(LagInfo));   // freed separately in the destructor
     if (e != cudaSuccess) pl->li_dev = nullptr;
-    AL(pl->trace, nt * j.nopit);
-    AL(pl->bparams, nt * kBleachStride);
+    AS(pl->trace, nt * j.nopit);
+    AS(pl->bparams, nt * kBleachStride);
     AL(pl->snap_pos, kMaxSnap);
-    AL(pl->segtot, nt * pl->nseg);
-    AL(pl->snap_part, nt * j.nsnap);
-    AL(pl->segbad, nt * pl->nseg);
-    AL(pl->snap_bad, nt * j.nsnap);
-    AL(pl->mon, np * chanum);
-    AL(pl->blkmon, np);
-    AL(pl->s1, np * pl->nbseg * (kBlkSegLog + 1));
-    AL(pl->s2, np * pl->nbseg * (kBlkSegLog + 1));
-    AL(pl->segsum, np * pl->nbseg);
-    AL(pl->blk_ind, np);
-    AL(pl->blk_ok, np);
-    AL(pl->stats, corr_stats_floats(j));
-    AL(pl->streams, corr_stream_floats(j));
-    AL(pl->s0, level0_stream_floats(j));
-    AL(pl->acf_int, np * chanum);
-    AL(pl->var_int, np * chanum);
+    AS(pl->segtot, nt * pl->nseg);
+    AS(pl->snap_part, nt * j.nsnap);
+    AS(pl->segbad, nt * pl->nseg);
+    AS(pl->snap_bad, nt * j.nsnap);
+    AS(pl->mon, np * chanum);
+    AS(pl->blkmon, np);
+    AS(pl->s1, np * pl->nbseg * (kBlkSegLog + 1));
+    AS(pl->s2, np * pl->nbseg * (kBlkSegLog + 1));
+    AS(pl->segsum, np * pl->nbseg);
+    AS(pl->blk_ind, np);
+    AS(pl->blk_ok, np);
+    AS(pl->stats, corr_stats_floats(j));
+    AS(pl->streams, corr_stream_floats(j));
+    AS(pl->s0, level0_stream_floats(j));
+    AS(pl->acf_int, np * chanum);
+    AS(pl->var_int, np * chanum);
     AL(pl->lagtime, chanum);
     AL(pl->dev_err, 1);
     if (j.bleach == IMFCS_BLEACH_POLYNOMIAL) {
@@ -435,31 +468,41 @@ int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h,
         AL(pl->basis, (size_t)(j.poly_order + 1) * j.num);
     }
     if (cfg->gls) {
-        AL(pl->bprod, np * (chanum - 1) * (size_t)pl->pnum_max);
-        AL(pl->linv, np * (size_t)(chanum - 1) * chanum / 2);
-        AL(pl->ytrans, np * (chanum - 1));
-        AL(pl->gls_ok, np);
+        AS(pl->bprod, np * (chanum - 1) * (size_t)pl->pnum_max);
+        AS(pl->linv, np * (size_t)(chanum - 1) * chanum / 2);
+        AS(pl->ytrans, np * (chanum - 1));
+        AS(pl->gls_ok, np);
     }
     if (cfg->do_fit || cfg->bayes) {
-        AL(pl->fit_y, np * pl->nfitpts);
-        AL(pl->fit_w, np * pl->nfitpts);
+        AS(pl->fit_y, np * pl->nfitpts);
+        AS(pl->fit_w, np * pl->nfitpts);
         AL(pl->fit_x, pl->nfitpts);
         AL(pl->fit_init, IMFCS_NPARAM);
-        AL(pl->fit_par, np * IMFCS_NPARAM);
-        AL(pl->fit_chi2, np);
-        AL(pl->fit_hess, np * IMFCS_NPARAM * IMFCS_NPARAM);
-        AL(pl->fit_state, np);
-        AL(pl->fit_iter, np);
+        AS(pl->fit_par, np * IMFCS_NPARAM);
+        AS(pl->fit_chi2, np);
+        AS(pl->fit_hess, np * IMFCS_NPARAM * IMFCS_NPARAM);
+        AS(pl->fit_state, np);
+        AS(pl->fit_iter, np);
         AL(pl->lm_counter, 1);
     }
     if (cfg->bayes) {
-        AL(pl->logp1, np);
-        AL(pl->logp2, np);
+        AS(pl->logp1, np);
+        AS(pl->logp2, np);
         AL(pl->bfit_init1, IMFCS_NPARAM);
         AL(pl->bfit_init2, IMFCS_NPARAM);
-        AL(pl->bfit_res, np * IMFCS_NPARAM);
+        AS(pl->bfit_res, np * IMFCS_NPARAM);
     }
 #undef AL
+#undef AS
+    // the scratch arena (a batch binds its own instead)
+    if (e == cudaSuccess && !external_scratch) {
+        e = cudaMalloc(&pl->own_arena, pl->scratch_need);
+        if (e != cudaSuccess) pl->own_arena = nullptr;
+        else {
+            pl->bytes += pl->scratch_need;
+            pl->bind_scratch(pl->own_arena);
+        }
+    }
     if (e != cudaSuccess) {
         set_error(cuda_msg(e, "plan allocation"));
         delete pl;
@@ -1186,4 +1229,96 @@ extern "C" int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max
         }
     }
     return n;
+}
+
+// ---------------------------------------------------------------------------
+// Correlator tile of the level chain and its autotuner (no counterpart in
+// the reference, whose kernels use fixed 16x16 blocks, agpufitjni.cu:5521).
+// ---------------------------------------------------------------------------
+namespace imfcs {
+size_t plan_scratch_need(const imfcs_plan *pl) { return pl->scratch_need; }
+void plan_bind_scratch(imfcs_plan *pl, void *base) { pl->bind_scratch(base); }
+const int *plan_dev_err(const imfcs_plan *pl) { return pl->dev_err; }
+
+// The correlator alone over the level-0 stream, monitors and blocking of the
+// plan's last execution on dev_stack (same scratch, same outputs).
+int plan_corr_only(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *dev_out, cudaStream_t s)
+{
+    const Job &j = pl->job;
+    double *acf = dev_out->acf ? dev_out->acf : pl->acf_int;
+    double *var = dev_out->var ? dev_out->var : pl->var_int;
+    CK(launch_corr(j, pl->li_dev, dev_stack, pl->bparams, pl->basis, pl->s0, pl->mon, pl->blk_ind, acf, var,
+                   dev_out->sd, dev_out->nb_mean, dev_out->nb_cov, pl->bprod, pl->pnum_max, pl->stats, pl->streams,
+                   pl->cfg.gls, pl->dev_err, s));
+    return 0;
+}
+}  // namespace imfcs
+
+extern "C" int imfcs_plan_set_corr_tile(imfcs_plan *pl, int cta, int seg_extra)
+{
+    if (!pl) { set_error("null plan"); return 1; }
+    if ((cta != 32 && cta != 64) || seg_extra < 0 || seg_extra > 2) {
+        set_error("correlator tile: cta must be 32 or 64 and seg_extra 0..2");
+        return 1;
+    }
+    pl->job.c2_cta = cta;
+    pl->job.c2_seg_extra = seg_extra;
+    return 0;
+}
+
+extern "C" int imfcs_plan_get_corr_tile(const imfcs_plan *pl, int *cta, int *seg_extra)
+{
+    if (!pl || !cta || !seg_extra) { set_error("null argument"); return 1; }
+    *cta = pl->job.c2_cta ? pl->job.c2_cta : 64;
+    *seg_extra = pl->job.c2_seg_extra;
+    return 0;
+}
+
+extern "C" int imfcs_plan_autotune(imfcs_plan *pl, const uint16_t *dev_stack, const imfcs_outputs *dev_out,
+                                   void *stream, imfcs_corr_tile *trials, int max_trials, int *n_trials)
+{
+    if (!pl || !dev_stack || !dev_out) { set_error("null argument"); return 1; }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_trials) *n_trials = 0;
+    // one full execution leaves the correlator's inputs in the scratch
+    const bool timing = pl->timing;
+    pl->timing = false;
+    int rc = plan_execute_any(pl, dev_stack, dev_out, stream);
+    pl->timing = timing;
+    if (rc) return 1;
+    if (pl->nb_only || !corr2_supported(pl->job)) return 0;   // no chain: nothing to tune
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int ctas[2] = {64, 32};
+    const int extras[3] = {0, 1, 2};
+    float best = 0.f;
+    int best_cta = 64, best_extra = 0, n = 0;
+    for (int ci = 0; ci < 2 && !rc; ci++)
+        for (int xi = 0; xi < 3 && !rc; xi++) {
+            pl->job.c2_cta = ctas[ci];
+            pl->job.c2_seg_extra = extras[xi];
+            // warm-up, then the median of three launches
+            if (plan_corr_only(pl, dev_stack, dev_out, s)) { rc = 1; break; }
+            float t[3];
+            for (int r = 0; r < 3 && !rc; r++) {
+                cudaError_t e = cudaEventRecord(e0, s);
+                if (e == cudaSuccess && plan_corr_only(pl, dev_stack, dev_out, s)) { rc = 1; break; }
+                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], e0, e1);
+                if (e != cudaSuccess) { set_error(cuda_msg(e, "autotune timing")); rc = 1; }
+            }
+            if (rc) break;
+            std::sort(t, t + 3);
+            if (trials && n < max_trials) trials[n] = {ctas[ci], extras[xi], t[1]};
+            n++;
+            if (n == 1 || t[1] < best) { best = t[1]; best_cta = ctas[ci]; best_extra = extras[xi]; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pl->job.c2_cta = best_cta;
+    pl->job.c2_seg_extra = best_extra;
+    if (n_trials) *n_trials = n < max_trials ? n : max_trials;
+    return rc;
 }

@@ -546,6 +546,9 @@ template __global__ void corr_kernel<true>(Job, const LagInfo *, const void *, c
 // kernel covers the rest (blocks shorter than 16 samples).
 // ---------------------------------------------------------------------------
 bool corr2_supported(const Job &j);
+bool corrg_supported(const Job &j);
+cudaError_t launch_corrg(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
+                         const CorrOut &o, cudaStream_t stream);
 cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
                          const CorrOut &o, float *streams, cudaStream_t stream);
 
@@ -595,6 +598,7 @@ cudaError_t launch_corr(const Job &j, const LagInfo *li, const void *stack, cons
     o.acf = acf; o.var = var; o.sd = sd; o.nb_mean = nb_mean; o.nb_cov = nb_cov;
     o.bprod = bprod; o.pnum_stride = pnum_stride; o.stats = stats; o.gls = gls; o.err = err;
     if (corr2_supported(j)) return launch_corr2(j, li, s0, mon, blk_ind, o, streams, stream);
+    if (corrg_supported(j)) return launch_corrg(j, li, s0, mon, blk_ind, o, stream);
     TmaGeom g = tma_geometry(j, stack);
     CUtensorMap map;
     memset(&map, 0, sizeof(map));

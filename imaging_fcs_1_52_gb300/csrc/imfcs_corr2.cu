@@ -33,7 +33,8 @@
 
 namespace imfcs {
 
-constexpr int kC2Threads = 64;
+constexpr int kC2Threads = 64;       // pixels per CTA unless the tile says 32
+constexpr int kMaxSegExtra = 3;
 constexpr int kHeadFields = (kP + 1) + 8;                   // first-level heads d = 0..16, second-level d = 9..16
 
 // Arguments shared by the pair, tail and finalise kernels.
@@ -42,7 +43,7 @@ struct C2Args {
     const float4 *mon;        // [pix][chanum] (a, b, dm, Dm)
     const int *blk_ind;       // [pix]
     const LagInfo *li;
-    int npix, chanum, q, num;
+    int npix, chanum, p, q, num;
     int numbin[kMaxLevels];
     int seg_log[kMaxLevels];  // frame segment (log2) of the kernel owning each level
     size_t stat_stride;       // floats per segment in o.stats
@@ -388,16 +389,16 @@ __device__ __forceinline__ void c2_pair_body(const C2Args &a, Src &src, float *o
         for (int l = 0; l < 8; l++) c2_add_total(c, p.lagS + l, R.accS[l]);
 }
 
-template <bool CCF, bool FIRST17, bool TWO>
-__global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const float *inA, const float *inB,
-                                                             float *outA, float *outB, int k)
+template <bool CCF, bool FIRST17, bool TWO, int NT>
+__global__ void __launch_bounds__(NT) c2_pair_kernel(C2Args a, const float *inA, const float *inB,
+                                                     float *outA, float *outB, int k)
 {
     constexpr int NL = (FIRST17 ? kP + 1 : 8) + (TWO ? 8 : 0);
-    __shared__ float heads_sm[kHeadFields * kC2Threads];
+    __shared__ float heads_sm[kHeadFields * NT];
     // block statistics and monitors of this pass's lags in shared memory: the
     // read-modify-writes at block ends stay on chip; written back at the end
-    __shared__ float sst[NL * kStatN * kC2Threads];
-    __shared__ float2 smon[NL * kC2Threads];
+    __shared__ float sst[NL * kStatN * NT];
+    __shared__ float2 smon[NL * NT];
     const int nt = blockDim.x, tid = threadIdx.x;
     const int pix = blockIdx.x * nt + tid, seg = blockIdx.y;
     if (pix >= a.npix) return;          // no block-wide synchronisation below
@@ -425,15 +426,15 @@ __global__ void __launch_bounds__(kC2Threads) c2_pair_kernel(C2Args a, const flo
 // keeps a ring of its last 32 samples in shared memory and its lags' block
 // sums and block statistics in registers; the statistics are written once.
 // ---------------------------------------------------------------------------
-template <bool CCF>
-__global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
+template <bool CCF, int NT>
+__global__ void __launch_bounds__(NT) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
 {
-    __shared__ float ring_sm[(CCF ? 2 : 1) * 32 * kC2Threads];
+    __shared__ float ring_sm[(CCF ? 2 : 1) * 32 * NT];
     const int tid = threadIdx.x;
-    const int pix = blockIdx.x * kC2Threads + tid, seg = blockIdx.y, k = k0 + blockIdx.z;
+    const int pix = blockIdx.x * NT + tid, seg = blockIdx.y, k = k0 + blockIdx.z;
     if (pix >= a.npix || k >= a.q) return;          // no block-wide synchronisation below
     float *rb = ring_sm + tid;
-    float *ra = CCF ? ring_sm + 32 * kC2Threads + tid : rb;
+    float *ra = CCF ? ring_sm + 32 * NT + tid : rb;
     if (!CCF) inA = inB;
     C2Ctx c;
     c2_ctx(c, a, pix, seg, k);
@@ -507,29 +508,29 @@ __global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const flo
         for (int u = 0; u < 8; u++) {
             const int n = nb + u;
             if (n >= nend) break;
-            rb[(n & 31) * kC2Threads] = vb[u];
-            if (CCF) ra[(n & 31) * kC2Threads] = va[u];
+            rb[(n & 31) * NT] = vb[u];
+            if (CCF) ra[(n & 31) * NT] = va[u];
             const int y = n - 16;
             if (y < ys0) continue;
             if (y == ys0) {
                 float h = 0.f;
 #pragma unroll
                 for (int i = 0; i < 16; i++) {
-                    h += rb[((y + i) & 31) * kC2Threads];
+                    h += rb[((y + i) & 31) * NT];
                     if (i + 1 >= 9) head[i + 1 - 9] = h;
                 }
             }
-            const float x0 = ra[(y & 31) * kC2Threads];
+            const float x0 = ra[(y & 31) * NT];
 #pragma unroll
-            for (int l = 0; l < 8; l++) acc[l] = fmaf(x0, rb[((y + 9 + l) & 31) * kC2Threads], acc[l]);
+            for (int l = 0; l < 8; l++) acc[l] = fmaf(x0, rb[((y + 9 + l) & 31) * NT], acc[l]);
             b0 += x0;
-            b1 += rb[(y & 31) * kC2Threads];
+            b1 += rb[(y & 31) * NT];
             if (((y + 1) & (L - 1)) == 0) {
                 // heads of the next block: sums of the delayed samples y+1 .. y+d
                 float nh[8], h = 0.f;
 #pragma unroll
                 for (int i = 1; i <= 16; i++) {
-                    h += rb[((y + i) & 31) * kC2Threads];
+                    h += rb[((y + i) & 31) * NT];
                     if (i >= 9) nh[i - 9] = h;
                 }
                 const int z = y / L;
@@ -571,6 +572,150 @@ __global__ void __launch_bounds__(kC2Threads) c2_tail_kernel(C2Args a, const flo
 }
 
 // ---------------------------------------------------------------------------
+// Generic-P level kernel (the plugin's P = 32, java:1022-1024): one (pixel,
+// level k, group of up to 8 delays) per thread over the whole frame range
+// (one segment).  Level 0 has delays 0..P, level k >= 1 delays P/2+1..P
+// (java:7391-7424).  The thread builds its level-k samples from the level-0
+// stream (sums of 2^k samples, pairwise within groups of 8), keeps a ring of
+// its last 2P samples in shared memory and its delays' block sums and block
+// statistics in registers, like the tail kernel.
+// ---------------------------------------------------------------------------
+template <bool CCF, int P>
+__global__ void __launch_bounds__(64) cg_kernel(C2Args a, const float *inA, const float *inB)
+{
+    constexpr int NT = 64;
+    constexpr int RS = 2 * P;                       // ring (power of two, > the largest delay)
+    constexpr int G0 = (P + 1 + 7) / 8;             // level-0 groups: delays 0..P
+    constexpr int GK = P / 2 / 8;                   // groups of an upper level
+    __shared__ float ring_sm[(CCF ? 2 : 1) * RS * NT];
+    const int tid = threadIdx.x;
+    const int pix = blockIdx.x * NT + tid;
+    const int gy = blockIdx.y;
+    int k, dlo, nd;
+    if (gy < G0) { k = 0; dlo = 8 * gy; nd = min(8, P + 1 - dlo); }
+    else { k = 1 + (gy - G0) / GK; dlo = P / 2 + 1 + 8 * ((gy - G0) % GK); nd = 8; }
+    if (pix >= a.npix || k >= a.q) return;          // no block-wide synchronisation below
+    float *rb = ring_sm + tid;
+    float *ra = CCF ? ring_sm + RS * NT + tid : rb;
+    if (!CCF) inA = inB;
+    C2Ctx c;
+    c2_ctx(c, a, pix, 0, k);
+    const int nkk = a.numbin[k], nk0 = a.numbin[0];
+    const int m = 1 << k;
+    const int lag0 = k == 0 ? dlo : (P + 1) + (k - 1) * (P / 2) + (dlo - (P / 2 + 1));
+    const int dmax = dlo + nd - 1;
+    const int lk = c.ind - k;
+    const int L = lk > 0 ? (1 << lk) : 1;
+
+    float ma[8], mb[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) {
+        const float4 mm = __ldg(&c.mon[lag0 + min(l, nd - 1)]);
+        ma[l] = mm.x;
+        mb[l] = mm.y;
+    }
+    float acc[8], head[8], thi[8], tlo[8], S1[8], S2[8], rr[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) acc[l] = head[l] = thi[l] = tlo[l] = S1[l] = S2[l] = rr[l] = 0.f;
+    float b0 = 0.f, b1 = 0.f;
+
+    // samples 0 .. nkk - 1 + dmax (samples from nkk on are zero)
+    const int nend = nkk + dmax;
+#pragma unroll 1
+    for (int n = 0; n < nend; n++) {
+        float vb = 0.f, va = 0.f;
+        if (n < nkk) {
+            for (int q0 = n * m; q0 < n * m + m; q0 += 8) {
+                float wb[8], wa[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const int q = q0 + i;
+                    const bool in = i < m && q < nk0;
+                    wb[i] = in ? __ldg(&inB[(size_t)q * a.npix + pix]) : 0.f;
+                    wa[i] = (CCF && in) ? __ldg(&inA[(size_t)q * a.npix + pix]) : 0.f;
+                }
+#pragma unroll
+                for (int w = 1; w < 8; w *= 2)
+#pragma unroll
+                    for (int i = 0; i < 8; i += 2 * w) {
+                        wb[i] += wb[i + w];
+                        wa[i] += wa[i + w];
+                    }
+                vb += wb[0];
+                va += wa[0];
+            }
+        }
+        rb[(n & (RS - 1)) * NT] = vb;
+        if (CCF) ra[(n & (RS - 1)) * NT] = va;
+        const int y = n - dmax;
+        if (y < 0) continue;
+        if (y == 0) {
+            // heads of the first block: sums of the delayed samples 0 .. d-1
+            float h = 0.f;
+#pragma unroll
+            for (int l = 0; l < 8; l++) head[l] = 0.f;
+            for (int i = 0; i < dmax; i++) {
+                h += rb[(i & (RS - 1)) * NT];
+#pragma unroll
+                for (int l = 0; l < 8; l++)
+                    if (dlo + l == i + 1) head[l] = h;
+            }
+        }
+        const float x0 = ra[(y & (RS - 1)) * NT];
+#pragma unroll
+        for (int l = 0; l < 8; l++) acc[l] = fmaf(x0, rb[((y + dlo + l) & (RS - 1)) * NT], acc[l]);
+        b0 += x0;
+        b1 += rb[(y & (RS - 1)) * NT];
+        if (((y + 1) & (L - 1)) == 0) {
+            // heads of the next block: sums of the delayed samples y+1 .. y+d
+            float nh[8], h = 0.f;
+#pragma unroll
+            for (int l = 0; l < 8; l++) nh[l] = 0.f;
+            for (int i = 1; i <= dmax; i++) {
+                h += rb[((y + i) & (RS - 1)) * NT];
+#pragma unroll
+                for (int l = 0; l < 8; l++)
+                    if (dlo + l == i) nh[l] = h;
+            }
+            const int z = y / L;
+            const bool stat = z < c.pnum;
+#pragma unroll
+            for (int l = 0; l < 8; l++) {
+                const float D = b1 - head[l] + nh[l];
+                const float Pz = (acc[l] - mb[l] * b0 - ma[l] * D + (float)L * ma[l] * mb[l]) / (float)L;
+                ff t = {thi[l], tlo[l]};
+                ff_add(t, acc[l]);
+                thi[l] = t.hi;
+                tlo[l] = t.lo;
+                if (stat && l < nd) {
+                    if (z == 0) rr[l] = Pz;
+                    const float dv = Pz - rr[l];
+                    S1[l] += dv;
+                    S2[l] = fmaf(dv, dv, S2[l]);
+                    if (c.gls && lag0 + l >= 1)
+                        c.bprod[((size_t)pix * (c.chanum - 1) + (lag0 + l - 1)) * c.pnum_stride + z] = Pz;
+                }
+                head[l] = nh[l];
+                acc[l] = 0.f;
+            }
+            b0 = 0.f;
+            b1 = 0.f;
+        }
+    }
+#pragma unroll
+    for (int l = 0; l < 8; l++) {
+        if (l >= nd) break;
+        ff t = {thi[l], tlo[l]};
+        ff_add(t, acc[l]);
+        stat_ref(c.stats, c.npix, lag0 + l, 0, pix) = t.hi;
+        stat_ref(c.stats, c.npix, lag0 + l, 1, pix) = t.lo;
+        stat_ref(c.stats, c.npix, lag0 + l, 2, pix) = S1[l];
+        stat_ref(c.stats, c.npix, lag0 + l, 3, pix) = S2[l];
+        stat_ref(c.stats, c.npix, lag0 + l, 4, pix) = rr[l];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Finalise: segments combined per (pixel, lag): product totals, block
 // statistics brought to one shift (FP64), outputs as calculateCF
 // (java:9491-9531).
@@ -584,7 +729,7 @@ __global__ void c2_finalize_kernel(C2Args a)
     const int lag = i / a.npix, pix = i % a.npix;
     const int ind = a.blk_ind[pix];
     const int pnum = a.li->pnum_by_ind[ind];
-    const int level = lag <= kP ? 0 : 1 + (lag - (kP + 1)) / 8;
+    const int level = lag <= a.p ? 0 : 1 + (lag - (a.p + 1)) / (a.p / 2);
     const int sl = a.seg_log[level];
     const int nseg = (a.num + (1 << sl) - 1) >> sl;
     double A = 0.0, S1 = 0.0, S2 = 0.0, r = 0.0;
@@ -627,6 +772,8 @@ __global__ void c2_finalize_kernel(C2Args a)
 // The chain needs blocks of at least 16 level-0 and 8 level-1 samples
 // (ind >= Q-1 >= 4).
 bool corr2_supported(const Job &j) { return j.p == kP && j.q >= 5; }
+// P = 32: the generic level kernel (any Q)
+bool corrg_supported(const Job &j) { return j.p == 32; }
 
 namespace {
 struct Plan2 {
@@ -639,7 +786,9 @@ struct Plan2 {
 Plan2 plan2(const Job &j)
 {
     Plan2 p;
-    const int base = max(j.blocknum - 1, j.q - 1);   // every pixel's block length divides 2^base frames
+    // every pixel's block length divides 2^base frames; the tile's segment
+    // extension multiplies every segment by 2^c2_seg_extra
+    const int base = max(j.blocknum - 1, j.q - 1) + min(max(j.c2_seg_extra, 0), kMaxSegExtra);
     p.npair = (j.q >= 7) ? 2 : 1;
     p.k_tail = 2 * p.npair;
     for (int k = 0; k < kMaxLevels; k++) p.seg_log[k] = 0;
@@ -663,6 +812,7 @@ int corr2_nseg(const Job &j) { return plan2(j).nseg_max; }
 
 int corr_kernel_count(const Job &j)
 {
+    if (corrg_supported(j)) return 2;
     if (!corr2_supported(j)) return 1;
     const Plan2 p = plan2(j);
     return p.npair + (p.k_tail < j.q ? 1 : 0) + 1;   // pair kernels, tail, finalise
@@ -686,6 +836,58 @@ size_t corr_stream_floats(const Job &j)
 // The corrected level-0 stream s0[trace][frame][pixel] (imfcs_stream.cu).
 size_t level0_stream_floats(const Job &j) { return (size_t)(j.is_ccf ? 2 : 1) * j.npix * j.num; }
 
+// One pair kernel of the chain: variant 0 = levels 0-1, 1 = two upper
+// levels, 2 = one upper level (the last).
+template <int NT>
+static void launch_pair(bool ccf, int variant, dim3 grid, cudaStream_t stream, const C2Args &a, const float *ia,
+                        const float *ib, float *oa, float *ob, int k)
+{
+    if (ccf) {
+        if (variant == 0) c2_pair_kernel<true, true, true, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+        else if (variant == 1) c2_pair_kernel<true, false, true, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+        else c2_pair_kernel<true, false, false, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+    } else {
+        if (variant == 0) c2_pair_kernel<false, true, true, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+        else if (variant == 1) c2_pair_kernel<false, false, true, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+        else c2_pair_kernel<false, false, false, NT><<<grid, NT, 0, stream>>>(a, ia, ib, oa, ob, k);
+    }
+}
+
+// The generic-P correlator: level kernel over the whole frame range, then
+// the finalise kernel (one segment).
+
+cudaError_t launch_corrg(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
+                         const CorrOut &o, cudaStream_t stream)
+{
+    C2Args a;
+    memset(&a, 0, sizeof(a));
+    a.o = o;
+    a.mon = mon;
+    a.blk_ind = blk_ind;
+    a.li = li;
+    a.npix = j.npix;
+    a.chanum = j.chanum;
+    a.p = j.p;
+    a.q = j.q;
+    a.num = j.num;
+    {
+        int nb = j.num;
+        for (int k = 0; k < j.q; k++) { a.numbin[k] = nb; nb /= 2; }
+    }
+    for (int k = 0; k < kMaxLevels; k++) a.seg_log[k] = 30;   // one segment
+    a.stat_stride = (size_t)j.chanum * kStatN * j.npix;
+    const float *s0a = s0, *s0b = j.is_ccf ? s0 + (size_t)j.npix * j.num : s0;
+    constexpr int P = 32;
+    const dim3 grid((j.npix + 63) / 64, (P + 1 + 7) / 8 + (j.q - 1) * (P / 16));
+    if (j.is_ccf) cg_kernel<true, P><<<grid, 64, 0, stream>>>(a, s0a, s0b);
+    else cg_kernel<false, P><<<grid, 64, 0, stream>>>(a, s0a, s0b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int n = j.npix * j.chanum;
+    c2_finalize_kernel<<<(n + 255) / 256, 256, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const float4 *mon, const int *blk_ind,
                          const CorrOut &o, float *streams, cudaStream_t stream)
 {
@@ -698,6 +900,7 @@ cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const
     a.li = li;
     a.npix = j.npix;
     a.chanum = j.chanum;
+    a.p = j.p;
     a.q = j.q;
     a.num = j.num;
     {
@@ -714,23 +917,17 @@ cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const
     float *s4a = s2a + tr * np * (j.num >> 2), *s4b = j.is_ccf ? s4a + np * (j.num >> 4) : s4a;
     cudaError_t e = cudaSuccess;
 
-    const int pgx = (j.npix + kC2Threads - 1) / kC2Threads;
+    const int nt = j.c2_cta == 32 ? 32 : kC2Threads;
+    const int pgx = (j.npix + nt - 1) / nt;
     for (int i = 0; i < pl.npair; i++) {
         const int k = 2 * i;
         const float *ia = i ? s2a : s0a, *ib = i ? s2b : s0b;
         float *oa = (k + 2 < j.q) ? (i ? s4a : s2a) : nullptr;
         float *ob = (k + 2 < j.q) ? (i ? s4b : s2b) : nullptr;
         const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k]) - 1) >> pl.seg_log[k]);
-        const bool two = k + 1 < j.q;
-        if (j.is_ccf) {
-            if (i == 0) c2_pair_kernel<true, true, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-            else if (two) c2_pair_kernel<true, false, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-            else c2_pair_kernel<true, false, false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-        } else {
-            if (i == 0) c2_pair_kernel<false, true, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-            else if (two) c2_pair_kernel<false, false, true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-            else c2_pair_kernel<false, false, false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, oa, ob, k);
-        }
+        const int variant = (i == 0) ? 0 : (k + 1 < j.q ? 1 : 2);
+        if (nt == 32) launch_pair<32>(j.is_ccf, variant, grid, stream, a, ia, ib, oa, ob, k);
+        else launch_pair<kC2Threads>(j.is_ccf, variant, grid, stream, a, ia, ib, oa, ob, k);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -738,8 +935,13 @@ cudaError_t launch_corr2(const Job &j, const LagInfo *li, const float *s0, const
         const int k0 = pl.k_tail;
         const float *ia = (k0 == 2) ? s2a : s4a, *ib = (k0 == 2) ? s2b : s4b;
         const dim3 grid(pgx, (j.num + (1 << pl.seg_log[k0]) - 1) >> pl.seg_log[k0], j.q - k0);
-        if (j.is_ccf) c2_tail_kernel<true><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
-        else c2_tail_kernel<false><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
+        if (nt == 32) {
+            if (j.is_ccf) c2_tail_kernel<true, 32><<<grid, 32, 0, stream>>>(a, ia, ib, k0);
+            else c2_tail_kernel<false, 32><<<grid, 32, 0, stream>>>(a, ia, ib, k0);
+        } else {
+            if (j.is_ccf) c2_tail_kernel<true, kC2Threads><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
+            else c2_tail_kernel<false, kC2Threads><<<grid, kC2Threads, 0, stream>>>(a, ia, ib, k0);
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -8,8 +8,20 @@
 // the unset zero-lag slot, java:9563-9573) and lamcov (correlations towards
 // zero, with the Java accumulation order, java:9592-9603), then the FP64
 // Cholesky with commons-math's thresholds (dataTransform, java:13705-13729)
-// and L^-1.  Products and first sums are FP32 with FP64 chunk accumulation;
-// the regularisation, Cholesky and inverse are FP64.
+// and L^-1.
+//
+// One pass over the centred samples e_xz gives, per lag pair (x >= y),
+// S1 = sum_z e_x e_y and S2 = sum_z (e_x e_y)^2 (FP32 per chunk of samples,
+// FP64 across chunks; each thread owns a 4x4 tile of pairs, so a sample
+// loaded from shared memory serves four pairs).  The shrinkage sums follow
+// without a second pass:
+//   sum_z (e_x^2 - c_xx)^2               = S2_xx - (pnum - 2) c_xx^2
+//   sum_z (e_x e_y / (sd_x sd_y) - r_xy)^2 = (S2_xy - (pnum - 2) c_xy^2) / (c_xx c_yy)
+// with c = S1 / (pnum - 1) and r = c / (sd_x sd_y).  Divisions by per-lag
+// quantities are multiplications by their reciprocals; the median is a
+// parallel rank selection; the Cholesky updates, L^-1 (one column per
+// thread) and L^-1 mcov (one row per thread) run in FP64 on the packed lower
+// triangle in shared memory.
 #include <math.h>
 
 #include "imfcs_internal.cuh"
@@ -18,240 +30,238 @@
 namespace imfcs {
 
 constexpr int kGlsThreads = 256;
-constexpr int kGlsZChunk = 128;
-constexpr int kMaxN1 = 96;   // chanum - 1 limit of this kernel
+constexpr int kGlsZChunk = 80;                  // samples per staged chunk
+constexpr int kGlsZStride = kGlsZChunk + 1;     // odd row stride: rows in distinct banks
+constexpr int kMaxN1 = 96;                      // chanum - 1 limit of this kernel
+constexpr int kGlsTile = 4;                     // pairs per thread: 4 x 4
 
-
-
-__device__ __forceinline__ void pair_of(int pr, int &x, int &y)
-{
-    int xx = (int)((sqrtf(8.f * pr + 1.f) - 1.f) * 0.5f);
-    while ((xx + 1) * (xx + 2) / 2 <= pr) xx++;
-    while (xx * (xx + 1) / 2 > pr) xx--;
-    x = xx;
-    y = pr - xx * (xx + 1) / 2;
-}
+__device__ __forceinline__ int tri(int r, int c) { return r * (r + 1) / 2 + c; }   // c <= r
 
 __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
 {
     extern __shared__ double gsh[];
     const int n1 = g.chanum - 1;
     const int npairs = n1 * (n1 + 1) / 2;
-    double *cm = gsh;                                  // [n1][n1] covmats / t_xy scratch
-    float *zb = (float *)(gsh + n1 * n1);              // [n1][kGlsZChunk]
-    __shared__ double mcov[kMaxN1], dmdm[kMaxN1], cdiag[kMaxN1], sdiag[kMaxN1];
-    __shared__ double red[kGlsThreads / 32];
-    __shared__ double s_median, s_lamvar, s_lamcov;
+    const int nrt = (n1 + kGlsTile - 1) / kGlsTile;    // tile rows
+    double *lp = gsh;                  // [npairs] S1 -> covariance/correlation -> regularised -> Cholesky factor
+    double *s2 = gsh + npairs;         // [npairs] S2 -> t_xy
+    float *eb = (float *)(gsh + 2 * npairs);   // [nrt*4][kGlsZStride] one chunk of centred samples
+    double *xinv = gsh + 2 * npairs;           // [npairs] L^-1 (after the sample passes)
+    __shared__ double mcov[kMaxN1], inv_dm[kMaxN1], cdiag[kMaxN1], isd[kMaxN1], sq[kMaxN1], rdiag[kMaxN1];
+    __shared__ double red[2][kGlsThreads / 32];
+    __shared__ double s_med[2], s_lamvar, s_lamcov, s_piv;
     __shared__ int s_fail;
 
     const int pix = blockIdx.x;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int pnum = g.pnum_by_ind[g.blk_ind[pix]];
     const float *bp = g.bprod + (size_t)pix * n1 * g.pnum_stride;
+    const double inv_pm1 = 1.0 / (double)(pnum - 1), inv_pnum = 1.0 / (double)pnum;
     if (tid < n1) {
-        float4 m = g.mon[(size_t)pix * g.chanum + tid + 1];
-        dmdm[tid] = (double)m.z * (double)m.w;
+        const float4 m = g.mon[(size_t)pix * g.chanum + tid + 1];
+        inv_dm[tid] = 1.0 / ((double)m.z * (double)m.w);
     }
     if (tid == 0) s_fail = 0;
+    for (int i = tid; i < npairs; i += kGlsThreads) { lp[i] = 0.0; s2[i] = 0.0; }
+    // rows past n1 of the staging buffer stay zero
+    for (int i = n1 * kGlsZStride + tid; i < nrt * kGlsTile * kGlsZStride; i += kGlsThreads) eb[i] = 0.f;
+    // mcov (java:9526-9531): sum of the blocked products, one warp per lag
+    for (int x = warp; x < n1; x += kGlsThreads / 32) {
+        double sum = 0.0;
+        for (int z = lane; z < pnum; z += 32) sum += (double)bp[(size_t)x * g.pnum_stride + z];
+        sum = warp_sum_d(sum);
+        if (lane == 0) mcov[x] = sum;
+    }
     __syncthreads();
-    // mcov (java:9526-9531)
+    if (tid < n1) mcov[tid] = mcov[tid] * inv_dm[tid] * inv_pnum;
+    __syncthreads();
+
+    // S1, S2 per pair: thread t owns tile (bx, by), bx >= by, of the pairs
+    // x in [4 bx, 4 bx + 4), y in [4 by, 4 by + 4)
+    const int ntiles = nrt * (nrt + 1) / 2;
+    for (int t0 = 0; t0 < ntiles; t0 += kGlsThreads) {
+        const int t = t0 + tid;
+        int bx = 0, by = 0;
+        if (t < ntiles) {
+            bx = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+            while ((bx + 1) * (bx + 2) / 2 <= t) bx++;
+            while (bx * (bx + 1) / 2 > t) bx--;
+            by = t - bx * (bx + 1) / 2;
+        }
+        for (int z0 = 0; z0 < pnum; z0 += kGlsZChunk) {
+            const int zn = min(kGlsZChunk, pnum - z0);
+            __syncthreads();
+            for (int i = tid; i < n1 * kGlsZChunk; i += kGlsThreads) {
+                const int x = i / kGlsZChunk, z = i - x * kGlsZChunk;
+                if (z < zn)
+                    eb[x * kGlsZStride + z] =
+                        (float)((double)bp[(size_t)x * g.pnum_stride + z0 + z] * inv_dm[x] - mcov[x]);
+            }
+            __syncthreads();
+            if (t >= ntiles) continue;
+            float a1[kGlsTile][kGlsTile], a2[kGlsTile][kGlsTile];
+#pragma unroll
+            for (int i = 0; i < kGlsTile; i++)
+#pragma unroll
+                for (int j = 0; j < kGlsTile; j++) { a1[i][j] = 0.f; a2[i][j] = 0.f; }
+            const float *ex = eb + (kGlsTile * bx) * kGlsZStride, *ey = eb + (kGlsTile * by) * kGlsZStride;
+            for (int z = 0; z < zn; z++) {
+                float vx[kGlsTile], vy[kGlsTile];
+#pragma unroll
+                for (int i = 0; i < kGlsTile; i++) { vx[i] = ex[i * kGlsZStride + z]; vy[i] = ey[i * kGlsZStride + z]; }
+#pragma unroll
+                for (int i = 0; i < kGlsTile; i++)
+#pragma unroll
+                    for (int j = 0; j < kGlsTile; j++) {
+                        const float u = vx[i] * vy[j];
+                        a1[i][j] += u;
+                        a2[i][j] = fmaf(u, u, a2[i][j]);
+                    }
+            }
+#pragma unroll
+            for (int i = 0; i < kGlsTile; i++)
+#pragma unroll
+                for (int j = 0; j < kGlsTile; j++) {
+                    const int x = kGlsTile * bx + i, y = kGlsTile * by + j;
+                    if (x < n1 && y <= x) {
+                        lp[tri(x, y)] += (double)a1[i][j];
+                        s2[tri(x, y)] += (double)a2[i][j];
+                    }
+                }
+        }
+    }
+    __syncthreads();
+    // covariance (java:9534-9542), standard deviations
+    for (int i = tid; i < npairs; i += kGlsThreads) lp[i] *= inv_pm1;
+    __syncthreads();
     if (tid < n1) {
-        double s = 0.0;
-        for (int z = 0; z < pnum; z++) s += (double)bp[(size_t)tid * g.pnum_stride + z] / dmdm[tid];
-        mcov[tid] = s / pnum;
+        const double c = lp[tri(tid, tid)];
+        cdiag[tid] = c;
+        isd[tid] = 1.0 / sqrt(c);
     }
     __syncthreads();
-    // covariance (java:9534-9542): pairs (x >= y)
-    constexpr int kMaxPairsPerThread = (kMaxN1 * (kMaxN1 + 1) / 2 + kGlsThreads - 1) / kGlsThreads;
-    double cacc[kMaxPairsPerThread];
-    for (int r = 0; r < kMaxPairsPerThread; r++) cacc[r] = 0.0;
-    for (int z0 = 0; z0 < pnum; z0 += kGlsZChunk) {
-        int zn = min(kGlsZChunk, pnum - z0);
-        for (int i = tid; i < n1 * kGlsZChunk; i += kGlsThreads) {
-            int x = i / kGlsZChunk, z = i % kGlsZChunk;
-            zb[i] = z < zn ? (float)((double)bp[(size_t)x * g.pnum_stride + z0 + z] / dmdm[x] - mcov[x]) : 0.f;
+    // median of the chanum diagonal entries incl. the zero-lag slot that
+    // stays 0 (java:9563-9573): rank selection, ties ordered by index
+    if (tid <= n1) {
+        const double v = tid == 0 ? 0.0 : cdiag[tid - 1];
+        int rank = 0;
+        for (int j = 0; j <= n1; j++) {
+            const double w = j == 0 ? 0.0 : cdiag[j - 1];
+            rank += (w < v) || (w == v && j < tid);
         }
-        __syncthreads();
-        for (int r = 0; r < kMaxPairsPerThread; r++) {
-            int pr = tid + r * kGlsThreads;
-            if (pr >= npairs) break;
-            int x, y;
-            pair_of(pr, x, y);
-            const float *ex = zb + x * kGlsZChunk, *ey = zb + y * kGlsZChunk;
-            float s = 0.f;
-            for (int z = 0; z < zn; z++) s = fmaf(ex[z], ey[z], s);
-            cacc[r] += (double)s;
-        }
-        __syncthreads();
+        const int c = n1 + 1;
+        const int pos1 = (c - 1) / 2, pos2 = c / 2;     // floor / ceil of (c - 1) / 2
+        if (rank == pos1) s_med[0] = v;
+        if (rank == pos2) s_med[1] = v;
     }
-    // covariance to cm (full symmetric)
-    for (int r = 0; r < kMaxPairsPerThread; r++) {
-        int pr = tid + r * kGlsThreads;
-        if (pr >= npairs) break;
-        int x, y;
-        pair_of(pr, x, y);
-        double v = cacc[r] / (pnum - 1);
-        cm[x * n1 + y] = v;
-        cm[y * n1 + x] = v;
-    }
-    __syncthreads();
-    if (tid < n1) { cdiag[tid] = cm[tid * n1 + tid]; sdiag[tid] = sqrt(cdiag[tid]); }
-    __syncthreads();
-    // median over chanum entries incl. the zero-lag slot that stays 0 (java:9563-9573)
-    if (tid == 0) {
-        double v[kMaxN1 + 1];
-        v[0] = 0.0;
-        for (int i = 0; i < n1; i++) v[i + 1] = cdiag[i];
-        for (int i = 1; i <= n1; i++) {
-            double t = v[i];
-            int jj = i - 1;
-            while (jj >= 0 && v[jj] > t) { v[jj + 1] = v[jj]; jj--; }
-            v[jj + 1] = t;
-        }
-        int c = n1 + 1;
-        double pos1 = floor((c - 1.0) / 2.0), pos2 = ceil((c - 1.0) / 2.0);
-        s_median = (pos1 == pos2) ? v[(int)pos1] : (v[(int)pos1] + v[(int)pos2]) / 2.0;
-    }
-    __syncthreads();
+    // t_xy and correlations; lamvar's and lamcov's sums
     const double f = (double)pnum / pow((double)pnum - 1.0, 3);
-    // shrinkage sums: per-x variance-of-variance, per-pair variance-of-correlation
-    double varnum[(kMaxN1 + kGlsThreads - 1) / kGlsThreads] = {0.0};
-    double tacc[kMaxPairsPerThread];
-    for (int r = 0; r < kMaxPairsPerThread; r++) tacc[r] = 0.0;
-    for (int z0 = 0; z0 < pnum; z0 += kGlsZChunk) {
-        int zn = min(kGlsZChunk, pnum - z0);
-        for (int i = tid; i < n1 * kGlsZChunk; i += kGlsThreads) {
-            int x = i / kGlsZChunk, z = i % kGlsZChunk;
-            zb[i] = z < zn ? (float)((double)bp[(size_t)x * g.pnum_stride + z0 + z] / dmdm[x] - mcov[x]) : 0.f;
+    const double pm2 = (double)(pnum - 2);
+    for (int i = tid; i < npairs; i += kGlsThreads) {
+        int x = (int)((sqrtf(8.f * i + 1.f) - 1.f) * 0.5f);
+        while ((x + 1) * (x + 2) / 2 <= i) x++;
+        while (x * (x + 1) / 2 > i) x--;
+        const int y = i - x * (x + 1) / 2;
+        const double c = lp[i];
+        const double t = s2[i] - pm2 * c * c;        // sum_z (e_x e_y - c_xy)^2 terms
+        if (x == y) {
+            s2[i] = t;                               // lamvar numerator term
+        } else {
+            const double k = isd[x] * isd[y];
+            s2[i] = t * k * k;                       // t_xy
+            lp[i] = c * k;                           // correlation
         }
-        __syncthreads();
-        if (tid < n1) {
-            float cxx = (float)cdiag[tid], s = 0.f;
-            for (int z = 0; z < zn; z++) { float e = zb[tid * kGlsZChunk + z]; float d = e * e - cxx; s = fmaf(d, d, s); }
-            varnum[0] += (double)s;
-        }
-        for (int r = 0; r < kMaxPairsPerThread; r++) {
-            int pr = tid + r * kGlsThreads;
-            if (pr >= npairs) break;
-            int x, y;
-            pair_of(pr, x, y);
-            if (y == x) continue;
-            const float *ex = zb + x * kGlsZChunk, *ey = zb + y * kGlsZChunk;
-            float isx = (float)(1.0 / sdiag[x]), isy = (float)(1.0 / sdiag[y]);
-            float cor = (float)(cm[x * n1 + y] / (sdiag[x] * sdiag[y]));
-            float s = 0.f;
-            for (int z = 0; z < zn; z++) { float d = ex[z] * isx * (ey[z] * isy) - cor; s = fmaf(d, d, s); }
-            tacc[r] += (double)s;
-        }
-        __syncthreads();
     }
-    // lamvar
+    __syncthreads();
+    if (tid == 0) {
+        const double med = (s_med[0] + s_med[1]) * 0.5;
+        s_med[0] = med;
+    }
     {
-        double num = (tid < n1) ? varnum[0] * f : 0.0;
-        double den = (tid < n1) ? (cdiag[tid] - s_median) * (cdiag[tid] - s_median) : 0.0;
+        double num = 0.0, den = 0.0;
+        if (tid < n1) num = s2[tri(tid, tid)] * f;
+        __syncthreads();                              // the median's average
+        if (tid < n1) {
+            const double d = cdiag[tid] - s_med[0];
+            den = d * d;
+        }
         num = warp_sum_d(num);
         den = warp_sum_d(den);
-        if ((tid & 31) == 0) red[tid >> 5] = num;
-        __syncthreads();
-        if (tid == 0) { double s = 0; for (int i = 0; i < kGlsThreads / 32; i++) s += red[i]; s_lamvar = s; }
-        __syncthreads();
-        if ((tid & 31) == 0) red[tid >> 5] = den;
+        if (lane == 0) { red[0][warp] = num; red[1][warp] = den; }
         __syncthreads();
         if (tid == 0) {
-            double s = 0; for (int i = 0; i < kGlsThreads / 32; i++) s += red[i];
-            double lv = fmin(1.0, s_lamvar / s);
-            s_lamvar = fmax(lv, 0.0);
+            double a = 0.0, b = 0.0;
+            for (int w = 0; w < kGlsThreads / 32; w++) { a += red[0][w]; b += red[1][w]; }
+            s_lamvar = fmax(fmin(1.0, a / b), 0.0);
         }
         __syncthreads();
     }
-    // lamcov: t_xy into cm's strictly upper triangle scratch (cm[y*n1+x], y<x), then
-    // the Java recursion T_y = (T_{y-1} + t_xy) f, numerator += T_y per x.
-    __syncthreads();
-    // keep covariance values needed later: store correlations first
-    for (int r = 0; r < kMaxPairsPerThread; r++) {
-        int pr = tid + r * kGlsThreads;
-        if (pr >= npairs) break;
-        int x, y;
-        pair_of(pr, x, y);
-        if (y == x) continue;
-        cm[y * n1 + x] = tacc[r];                    // upper: t_xy
-        cm[x * n1 + y] = cm[x * n1 + y] / (sdiag[x] * sdiag[y]);   // lower: cor_xy
-    }
-    __syncthreads();
+    // lamcov: per x, T_y = (T_{y-1} + t_xy) f summed over y < x
     {
         double num = 0.0, den = 0.0;
         if (tid < n1) {
-            int x = tid;
+            const int x = tid;
             double T = 0.0;
             for (int y = 0; y < x; y++) {
-                T = (T + cm[y * n1 + x]) * f;
+                T = (T + s2[tri(x, y)]) * f;
                 num += T;
-                double c = cm[x * n1 + y];
-                den += c * c;
+                const double r = lp[tri(x, y)];
+                den += r * r;
             }
         }
         num = warp_sum_d(num);
         den = warp_sum_d(den);
-        __syncthreads();
-        if ((tid & 31) == 0) red[tid >> 5] = num;
-        __syncthreads();
-        double tot_num = 0.0;
-        if (tid == 0) for (int i = 0; i < kGlsThreads / 32; i++) tot_num += red[i];
-        __syncthreads();
-        if ((tid & 31) == 0) red[tid >> 5] = den;
+        if (lane == 0) { red[0][warp] = num; red[1][warp] = den; }
         __syncthreads();
         if (tid == 0) {
-            double s = 0; for (int i = 0; i < kGlsThreads / 32; i++) s += red[i];
-            double lc = fmin(1.0, tot_num / s);
-            s_lamcov = fmax(lc, 0.0);
+            double a = 0.0, b = 0.0;
+            for (int w = 0; w < kGlsThreads / 32; w++) { a += red[0][w]; b += red[1][w]; }
+            s_lamcov = fmax(fmin(1.0, a / b), 0.0);
         }
         __syncthreads();
     }
-    // regularised covmats (java:9605-9615), FP64, full matrix in cm
-    const double lv = s_lamvar, lc = s_lamcov, med = s_median;
-    constexpr int kPer = (kMaxN1 * kMaxN1 + kGlsThreads - 1) / kGlsThreads;
-    double vals[kPer];
-#pragma unroll
-    for (int r = 0; r < kPer; r++) {
-        int i = tid + r * kGlsThreads;
-        vals[r] = 0.0;
-        if (i >= n1 * n1) continue;
-        int x = i / n1, y = i % n1;
-        if (x == y) continue;
-        int xl = x > y ? x : y, yl = x > y ? y : x;
-        double cor = cm[xl * n1 + yl];
-        double cmx = lv * med + (1 - lv) * cdiag[xl];
-        double cmy = lv * med + (1 - lv) * cdiag[yl];
-        vals[r] = (1 - lc) * cor * sqrt(cmx * cmy) / pnum;
+    // regularised covariance (java:9605-9615), FP64, packed lower triangle
+    const double lv = s_lamvar, lc = s_lamcov, med = s_med[0];
+    if (tid < n1) {
+        const double d = lv * med + (1.0 - lv) * cdiag[tid];
+        sq[tid] = sqrt(d);
+        rdiag[tid] = d * inv_pnum;
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kPer; r++) {
-        int i = tid + r * kGlsThreads;
-        if (i < n1 * n1 && (i / n1) != (i % n1)) cm[i] = vals[r];
+    for (int i = tid; i < npairs; i += kGlsThreads) {
+        int x = (int)((sqrtf(8.f * i + 1.f) - 1.f) * 0.5f);
+        while ((x + 1) * (x + 2) / 2 <= i) x++;
+        while (x * (x + 1) / 2 > i) x--;
+        const int y = i - x * (x + 1) / 2;
+        lp[i] = (x == y) ? rdiag[x] : (1.0 - lc) * lp[i] * sq[x] * sq[y] * inv_pnum;
     }
-    __syncthreads();
-    if (tid < n1) cm[tid * n1 + tid] = (lv * med + (1 - lv) * cdiag[tid]) / pnum;
     __syncthreads();
     if (g.covmats_out)
-        for (int i = tid; i < n1 * n1; i += kGlsThreads) g.covmats_out[(size_t)pix * n1 * n1 + i] = cm[i];
-    __syncthreads();
-    // Cholesky, commons-math order (java:13717): row-oriented on lt = cm (upper used)
+        for (int i = tid; i < n1 * n1; i += kGlsThreads) {
+            const int x = i / n1, y = i - x * n1;
+            g.covmats_out[(size_t)pix * n1 * n1 + i] = x >= y ? lp[tri(x, y)] : lp[tri(y, x)];
+        }
+    // Cholesky in commons-math's order (java:13717): pivot i, scale its
+    // column, then the trailing update A[q][p] -= A[q][i] A[p][i] (p <= q)
     for (int i = 0; i < n1; i++) {
         if (tid == 0) {
-            double d = cm[i * n1 + i];
-            if (!(d > 1e-10)) s_fail = 1;
-            cm[i * n1 + i] = sqrt(d);
+            const double d = lp[tri(i, i)];
+            if (!(d > 1e-10)) {
+                s_fail = 1;
+            } else {
+                const double r = sqrt(d);
+                lp[tri(i, i)] = r;
+                s_piv = 1.0 / r;
+            }
         }
         __syncthreads();
         if (s_fail) break;
-        double inv = 1.0 / cm[i * n1 + i];
-        for (int q = i + 1 + tid; q < n1; q += kGlsThreads) cm[i * n1 + q] *= inv;
+        for (int q = i + 1 + tid; q < n1; q += kGlsThreads) lp[tri(q, i)] *= s_piv;
         __syncthreads();
-        int m = n1 - i - 1;
-        for (int t = tid; t < m * m; t += kGlsThreads) {
-            int q = i + 1 + t / m, p = i + 1 + t % m;
-            if (p >= q) cm[q * n1 + p] -= cm[i * n1 + q] * cm[i * n1 + p];
+        for (int q = i + 1 + warp; q < n1; q += kGlsThreads / 32) {
+            const double aq = lp[tri(q, i)];
+            double *row = lp + tri(q, 0);
+            for (int p = i + 1 + lane; p <= q; p += 32) row[p] -= aq * lp[tri(p, i)];
         }
         __syncthreads();
     }
@@ -259,37 +269,41 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
         if (tid == 0) g.ok[pix] = 0;
         return;
     }
-    // L = lt^T: L[r][c] = cm[c*n1 + r] for c <= r.  L^-1 column by column.
-    float *lo = g.linv + (size_t)pix * npairs;
+    if (tid < n1) rdiag[tid] = 1.0 / lp[tri(tid, tid)];
+    __syncthreads();
+    // L^-1, column c on thread c: X[c][c] = 1/L[c][c],
+    // X[r][c] = -(sum_{m=c}^{r-1} L[r][m] X[m][c]) / L[r][r]
     if (tid < n1) {
-        const int col = tid;
-        double xv[kMaxN1];
-        for (int r = 0; r < col; r++) xv[r] = 0.0;
-        xv[col] = 1.0 / cm[col * n1 + col];
-        for (int r = col + 1; r < n1; r++) {
-            double s = 0.0;
-            for (int m = col; m < r; m++) s += cm[m * n1 + r] * xv[m];
-            xv[r] = -s / cm[r * n1 + r];
+        const int c = tid;
+        xinv[tri(c, c)] = rdiag[c];
+        for (int r = c + 1; r < n1; r++) {
+            const double *lr = lp + tri(r, 0);
+            double sum = 0.0;
+            for (int m = c; m < r; m++) sum = fma(lr[m], xinv[tri(m, c)], sum);
+            xinv[tri(r, c)] = -sum * rdiag[r];
         }
-        for (int r = col; r < n1; r++) lo[(size_t)r * (r + 1) / 2 + col] = (float)xv[r];
     }
-    // transformed data L^-1 mcov (forward substitution, FP64)
-    if (tid == 0) {
-        double yv[kMaxN1];
-        for (int r = 0; r < n1; r++) {
-            double s = mcov[r];
-            for (int m = 0; m < r; m++) s -= cm[m * n1 + r] * yv[m];
-            yv[r] = s / cm[r * n1 + r];
-            g.ytrans[(size_t)pix * n1 + r] = (float)yv[r];
-        }
-        g.ok[pix] = 1;
+    __syncthreads();
+    float *lo = g.linv + (size_t)pix * npairs;
+    for (int i = tid; i < npairs; i += kGlsThreads) lo[i] = (float)xinv[i];
+    // transformed data L^-1 mcov
+    if (tid < n1) {
+        const int r = tid;
+        const double *xr = xinv + tri(r, 0);
+        double sum = 0.0;
+        for (int c = 0; c <= r; c++) sum = fma(xr[c], mcov[c], sum);
+        g.ytrans[(size_t)pix * n1 + r] = (float)sum;
     }
+    if (tid == 0) g.ok[pix] = 1;
 }
 
 size_t gls_smem_bytes(int chanum)
 {
-    int n1 = chanum - 1;
-    return (size_t)n1 * n1 * sizeof(double) + (size_t)n1 * kGlsZChunk * sizeof(float);
+    const int n1 = chanum - 1;
+    const size_t npairs = (size_t)n1 * (n1 + 1) / 2;
+    const size_t rows = (size_t)((n1 + kGlsTile - 1) / kGlsTile) * kGlsTile;
+    const size_t stage = rows * kGlsZStride * sizeof(float);
+    return 2 * npairs * sizeof(double) + (stage > npairs * sizeof(double) ? stage : npairs * sizeof(double));
 }
 
 cudaError_t launch_gls(const GlsArgs &g, cudaStream_t stream)

@@ -82,8 +82,19 @@ void legendre_projection(int order, int nopit, int ave, double frametime, double
 void legendre_basis_table(int order, int num, double frametime, double uscale, double uoff,
                           float *table);
 
+// external_scratch: the plan's per-execution scratch is not allocated; a
+// batch binds an arena of plan_scratch_need bytes before each execution
 int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h, bool given_bleach,
-                   imfcs_plan **plan_out);
+                   imfcs_plan **plan_out, bool external_scratch = false);
 int plan_execute_any(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *dev_out, void *stream);
+bool corr2_supported(const Job &j);          // the level chain runs (P = 16, Q >= 5)
+
+// batch support (imfcs_batch.cu): per-execution scratch bytes, binding an
+// arena, the plan's device error flag, the correlator alone
+size_t plan_scratch_need(const imfcs_plan *pl);
+void plan_bind_scratch(imfcs_plan *pl, void *base);
+const int *plan_dev_err(const imfcs_plan *pl);
+const Job &plan_job(imfcs_plan *pl);
+int plan_corr_only(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *dev_out, cudaStream_t s);
 
 }  // namespace imfcs

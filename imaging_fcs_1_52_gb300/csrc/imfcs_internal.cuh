@@ -23,7 +23,7 @@ constexpr int kMaxBlockLevels = 32;
 constexpr int kMaxSnap = 3 * kMaxChan + 8;
 constexpr int kTile = 32;          // output pixels per correlator CTA (one warp lane each)
 constexpr int kChunk = 128;        // frames staged per correlator step
-constexpr int kP = 16;             // correlator P handled by the kernels
+constexpr int kP = 16;             // correlator P of the level chain (P = 32: the generic level kernel)
 constexpr int kHist = kP;          // window history kept per level
 constexpr int kMaxPoly = 8;        // polynomial bleach order (java BCmaxorder = 8)
 constexpr int kBleachStride = 16;  // floats per trace in the bleach-parameter array
@@ -57,6 +57,10 @@ struct Job {
     int blocknum;                 // floor(log2(mtab[1])) - 2
     // lag tables (device copies live in constant memory per launch via Job)
     int nsnap;
+    // correlator tile of the level chain (chosen by the autotuner): pixels
+    // per CTA (32 or 64; 0 = 64) and frame segments 2^c2_seg_extra times the
+    // shortest legal segment
+    int c2_cta, c2_seg_extra;
 };
 
 // Lag tables, snapshot positions and per-lag snapshot indices, stored in a

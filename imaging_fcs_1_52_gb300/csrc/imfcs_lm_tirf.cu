@@ -93,7 +93,29 @@ __device__ __noinline__ double tirf_d(double inv_N, double D, double G, const Ti
 // PSF) or an axial factor different from 1 in FP64 (SPIM) take the FP64
 // model instead.
 constexpr int kSeriesN = 16;
-__constant__ float kErfHi[kSeriesN], kErfLo[kSeriesN], kEm1Hi[kSeriesN], kEm1Lo[kSeriesN];
+
+// The series coefficients as float-float (hi = the float nearest the FP64
+// value, lo = the float nearest the remainder), evaluated at compile time.
+struct SeriesTab {
+    float eh[kSeriesN], el[kSeriesN], qh[kSeriesN], ql[kSeriesN];
+};
+constexpr SeriesTab make_series_tab()
+{
+    SeriesTab t{};
+    const double two_sqrtpi = 1.1283791670955125739;   // 2 / sqrt(pi)
+    double fact = 1.0;                                 // n!
+    for (int n = 0; n < kSeriesN; n++) {
+        if (n > 0) fact *= n;
+        const double en = ((n & 1) ? -1.0 : 1.0) * two_sqrtpi / (fact * (2 * n + 1));
+        const double qn = ((n & 1) ? -1.0 : 1.0) / (fact * (n + 1));
+        t.eh[n] = (float)en;
+        t.el[n] = (float)(en - (double)t.eh[n]);
+        t.qh[n] = (float)qn;
+        t.ql[n] = (float)(qn - (double)t.qh[n]);
+    }
+    return t;
+}
+__constant__ SeriesTab kSeries = make_series_tab();
 
 __device__ __forceinline__ f2 ff_const(const float *hi, const float *lo, int n) { return {hi[n], lo[n]}; }
 
@@ -104,11 +126,11 @@ __device__ __forceinline__ bool tirf_lat_ff(float a, f2 p0, f2 ip0, f2 &L)
     const f2 u = f2_mul_f(ip0, a);
     if (!(u.hi <= 1.f)) return false;
     const f2 x = f2_mul(u, u);
-    f2 pe = ff_const(kErfHi, kErfLo, kSeriesN - 1), pq = ff_const(kEm1Hi, kEm1Lo, kSeriesN - 1);
+    f2 pe = ff_const(kSeries.eh, kSeries.el, kSeriesN - 1), pq = ff_const(kSeries.qh, kSeries.ql, kSeriesN - 1);
 #pragma unroll
     for (int n = kSeriesN - 2; n >= 0; n--) {
-        pe = f2_add(f2_mul(pe, x), ff_const(kErfHi, kErfLo, n));
-        pq = f2_add(f2_mul(pq, x), ff_const(kEm1Hi, kEm1Lo, n));
+        pe = f2_add(f2_mul(pe, x), ff_const(kSeries.eh, kSeries.el, n));
+        pq = f2_add(f2_mul(pq, x), ff_const(kSeries.qh, kSeries.ql, n));
     }
     const f2 er = f2_mul(u, pe);                     // erf(u)
     const f2 m = f2_neg(f2_mul(x, pq));               // expm1(-u^2)
@@ -502,25 +524,6 @@ bool lm_tirf_applies(const FitArgs &a, bool tirf_zero_held)
 
 cudaError_t launch_lm_tirf(const FitArgs &a, int blocks, int threads, cudaStream_t s)
 {
-    // the series coefficients as float-float (hi = the float nearest the
-    // FP64 value, lo = the float nearest the remainder)
-    float eh[kSeriesN], el[kSeriesN], qh[kSeriesN], ql[kSeriesN];
-    const double two_sqrtpi = 1.1283791670955125739;   // 2 / sqrt(pi)
-    double fact = 1.0;                                 // n!
-    for (int n = 0; n < kSeriesN; n++) {
-        if (n > 0) fact *= n;
-        const double en = ((n & 1) ? -1.0 : 1.0) * two_sqrtpi / (fact * (2 * n + 1));
-        const double qn = ((n & 1) ? -1.0 : 1.0) / (fact * (n + 1));
-        eh[n] = (float)en;
-        el[n] = (float)(en - (double)eh[n]);
-        qh[n] = (float)qn;
-        ql[n] = (float)(qn - (double)qh[n]);
-    }
-    cudaError_t e = cudaMemcpyToSymbolAsync(kErfHi, eh, sizeof(eh), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kErfLo, el, sizeof(el), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kEm1Hi, qh, sizeof(qh), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(kEm1Lo, ql, sizeof(ql), 0, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
     lm_tirf_kernel<<<blocks, threads, 0, s>>>(a);
     return cudaGetLastError();
 }

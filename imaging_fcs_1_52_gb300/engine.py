@@ -274,6 +274,131 @@ class Plan:
         sp = None if stream is None else C.c_void_p(stream.cuda_stream)
         check(self._L.imfcs_plan_synchronize(self._h, sp), "imfcs_plan_synchronize")
 
+    def set_corr_tile(self, cta: int, seg_extra: int):
+        """Correlator tile of the level chain: cta pixels per CTA (32 or 64),
+        frame segments 2^seg_extra times the shortest legal one."""
+        check(self._L.imfcs_plan_set_corr_tile(self._h, int(cta), int(seg_extra)), "imfcs_plan_set_corr_tile")
+
+    def corr_tile(self) -> tuple[int, int]:
+        a, b = C.c_int(), C.c_int()
+        check(self._L.imfcs_plan_get_corr_tile(self._h, C.byref(a), C.byref(b)), "imfcs_plan_get_corr_tile")
+        return int(a.value), int(b.value)
+
+    def autotune(self, stack, outputs: dict, stream=None) -> list[dict]:
+        """Time the correlator at every tile on this stack, keep the fastest
+        (imfcs_plan_autotune); returns the trials."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        o = _outputs_struct({k: v.data_ptr() for k, v in outputs.items()})
+        trials = (_lib.CorrTile * 16)()
+        n = C.c_int()
+        check(self._L.imfcs_plan_autotune(self._h, C.c_void_p(stack.data_ptr()), C.byref(o),
+                                          C.c_void_p(s.cuda_stream), trials, 16, C.byref(n)), "imfcs_plan_autotune")
+        return [{"cta": t.cta, "seg_extra": t.seg_extra, "ms": float(t.ms)} for t in trials[:n.value]]
+
+
+def batch_configs(width: int, height: int, frames: int, binnings=(1, 2, 3, 4, 5),
+                  offsets=((0, 0), (1, 0), (2, 0), (0, 1), (1, 1), (2, 1), (0, 2), (1, 2), (2, 2)),
+                  **kw) -> list[FCSConfig]:
+    """One job per (binning, offset): non-overlapping binning (pixel step =
+    binning, as the diffusion law's "All" mode), cross-correlation of each
+    binned window with the window displaced by (dx, dy) input pixels
+    ((0, 0): autocorrelation); every job fits N, D, G with the model
+    constants of its binning."""
+    cfgs = []
+    psf = kw.pop("psf_um", 0.4)
+    pixel = kw.pop("pixel_um", 0.24)
+    for b in binnings:
+        for dx, dy in offsets:
+            cfgs.append(FCSConfig(width=width, height=height, frames=frames, binx=b, biny=b, cfx=dx, cfy=dy,
+                                  cst=model_constants(pixel_um=pixel, binx=b, biny=b, psf_um=psf, cfx=dx, cfy=dy),
+                                  **kw))
+    return cfgs
+
+
+class Batch:
+    """Several jobs over one stack as one CUDA graph (imfcs_batch_*)."""
+
+    def __init__(self, cfgs: list[FCSConfig], lanes: int = 1):
+        self.cfgs = list(cfgs)
+        self._L = _lib.load()
+        arr = (_lib.Config * len(self.cfgs))(*[c.to_c() for c in self.cfgs])
+        h = C.c_void_p()
+        check(self._L.imfcs_batch_create(arr, len(self.cfgs), int(lanes), C.byref(h)), "imfcs_batch_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.imfcs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def lanes(self) -> int:
+        return int(self._L.imfcs_batch_lanes(self._h))
+
+    @property
+    def scratch_bytes(self) -> int:
+        return int(self._L.imfcs_batch_scratch_bytes(self._h))
+
+    def kernel_launches(self) -> int:
+        return int(self._L.imfcs_batch_kernel_launches(self._h))
+
+    def job_info(self, i: int) -> dict:
+        v = [C.c_int() for _ in range(5)]
+        ms = C.c_float()
+        check(self._L.imfcs_batch_job_info(self._h, i, *[C.byref(x) for x in v], C.byref(ms)),
+              "imfcs_batch_job_info")
+        return {"npix": v[0].value, "chanum": v[1].value, "lane": v[2].value, "cta": v[3].value,
+                "seg_extra": v[4].value, "ms": float(ms.value)}
+
+    def alloc_device_outputs(self, device="cuda") -> list[dict]:
+        import torch
+        tmap = {"f8": torch.float64, "f4": torch.float32, "i4": torch.int32}
+        outs = []
+        for c in self.cfgs:
+            o = {}
+            for n in output_names(c):
+                dt, shp = _OUT_SPEC[n]
+                o[n] = torch.empty((c.npix, *shp(c.chanum)), dtype=tmap[dt], device=device)
+            outs.append(o)
+        return outs
+
+    def _outs(self, outputs: list[dict]):
+        arr = (_lib.Outputs * len(self.cfgs))()
+        for i, o in enumerate(outputs):
+            arr[i] = _outputs_struct({k: v.data_ptr() for k, v in o.items()})
+        return arr
+
+    def execute(self, stack, outputs: list[dict], stream=None):
+        """stack: CUDA uint16 tensor [frames][height][width]; outputs: one
+        dict of CUDA tensors per job.  Asynchronous on `stream`."""
+        import torch
+        assert stack.is_cuda and stack.is_contiguous()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        check(self._L.imfcs_batch_execute(self._h, C.c_void_p(stack.data_ptr()), self._outs(outputs),
+                                          C.c_void_p(s.cuda_stream)), "imfcs_batch_execute")
+        return outputs
+
+    def synchronize(self, stream=None):
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(self._L.imfcs_batch_synchronize(self._h, sp), "imfcs_batch_synchronize")
+
+    def autotune(self, stack, outputs: list[dict], max_lanes: int = 4, stream=None) -> list[float]:
+        """Tune the jobs' correlator tiles and the lane count on this stack
+        (imfcs_batch_autotune); returns the graph time per lane count."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        ms = (C.c_float * max_lanes)()
+        check(self._L.imfcs_batch_autotune(self._h, C.c_void_p(stack.data_ptr()), self._outs(outputs),
+                                           C.c_void_p(s.cuda_stream), int(max_lanes), ms), "imfcs_batch_autotune")
+        return [float(x) for x in ms]
+
 
 def run_host(stack: np.ndarray, cfg: FCSConfig) -> dict:
     plan = Plan(cfg)

@@ -252,6 +252,59 @@ IMFCS_API int imfcs_plan_kernel_launches(const imfcs_plan *plan);
 IMFCS_API int imfcs_plan_set_timing(imfcs_plan *plan, int enable);
 IMFCS_API int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max_stages);
 
+/* Correlator tile of the level chain (no counterpart in the reference, whose
+ * kernels use fixed 16x16 thread blocks, agpufitjni.cu:5521-5531): `cta`
+ * output pixels per CTA (32 or 64) and frame segments 2^seg_extra (0..2)
+ * times the shortest legal segment (the block length of the blocked
+ * variance).  Results agree to FP32 rounding of the per-segment sums. */
+typedef struct imfcs_corr_tile {
+    int cta;
+    int seg_extra;
+    float ms;                 /* median correlator time of the trial */
+} imfcs_corr_tile;
+IMFCS_API int imfcs_plan_set_corr_tile(imfcs_plan *plan, int cta, int seg_extra);
+IMFCS_API int imfcs_plan_get_corr_tile(const imfcs_plan *plan, int *cta, int *seg_extra);
+/* Autotuner: executes the plan once on dev_stack (outputs as
+ * imfcs_plan_execute), then times the correlator at every tile (median of
+ * three launches after one warm-up) and keeps the fastest.  Writes up to
+ * max_trials trials.  Synchronises `stream`. */
+IMFCS_API int imfcs_plan_autotune(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,
+                        void *stream, imfcs_corr_tile *trials, int max_trials, int *n_trials);
+
+/* Batches (no counterpart in the reference, which repeats one JNI call per
+ * binning, Imaging_FCS_1_52.java:11146-11166): several jobs -- binnings,
+ * cross-correlation offsets, ROIs of different sizes -- over one stack
+ * (every config has the same width, height, frames, first and num), run as
+ * one CUDA graph.  Jobs are spread over `lanes` concurrent branches of the
+ * graph; jobs of one lane run one after another on one scratch arena sized
+ * for the largest of them.  The graph is captured at the first execution
+ * and again whenever the stack, the outputs, the lanes or a tile change. */
+typedef struct imfcs_batch imfcs_batch;
+IMFCS_API int imfcs_batch_create(const imfcs_config *jobs, int n_jobs, int lanes, imfcs_batch **batch);
+IMFCS_API int imfcs_batch_destroy(imfcs_batch *batch);
+/* outs: n_jobs device output sets (as imfcs_plan_execute).  Asynchronous. */
+IMFCS_API int imfcs_batch_execute(imfcs_batch *batch, const uint16_t *dev_stack, const imfcs_outputs *outs,
+                        void *stream);
+/* Waits for `stream` and reports device-side errors of every job. */
+IMFCS_API int imfcs_batch_synchronize(imfcs_batch *batch, void *stream);
+/* Autotuner: tunes every job's correlator tile (imfcs_plan_autotune), times
+ * each job alone, then for 1..max_lanes lanes assigns jobs to lanes by
+ * longest measured time first and times the whole graph (median of three);
+ * keeps the fastest lane count.  lane_ms[l-1] receives the time with l lanes
+ * (max_lanes entries, 0 where the arenas did not fit in device memory).
+ * Synchronises `stream`. */
+IMFCS_API int imfcs_batch_autotune(imfcs_batch *batch, const uint16_t *dev_stack, const imfcs_outputs *outs,
+                         void *stream, int max_lanes, float *lane_ms);
+/* Per job: output pixels, channels, lane, correlator tile and measured time
+ * (ms, 0 before autotuning). */
+IMFCS_API int imfcs_batch_job_info(const imfcs_batch *batch, int job, int *npix, int *chanum, int *lane,
+                         int *cta, int *seg_extra, float *ms);
+IMFCS_API int imfcs_batch_lanes(const imfcs_batch *batch);
+/* Device bytes of the scratch arenas and of the jobs' own tables. */
+IMFCS_API size_t imfcs_batch_scratch_bytes(const imfcs_batch *batch);
+/* Kernels the graph launches per execution. */
+IMFCS_API int imfcs_batch_kernel_launches(const imfcs_batch *batch);
+
 /* Runs the whole path on a device-resident stack; outputs are device
  * pointers.  Asynchronous on `stream`. */
 IMFCS_API int imfcs_plan_execute(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,

@@ -67,6 +67,25 @@ def test_gls_fit_parity(bright):
     assert np.max(np.abs(cg[fin] - cr[fin]) / scale) <= 1e-4
 
 
+@pytest.mark.parametrize("kw", [{}, {"cfx": 1, "cfy": 0}], ids=["acf", "ccf10"])
+def test_gls_long_stack_parity(kw):
+    """20,000 frames: about 140 blocked products per lag, so the covariance
+    pass runs over several staged chunks of samples."""
+    st = brownian_stack(6, 5, 20000, seed=31, density=2.0, cps=3e4)
+    cfg = engine.FCSConfig(width=6, height=5, frames=20000, background=100, gls=True, **kw)
+    gpu, ref = run_both(st, cfg)
+    assert acf_deviation(gpu, ref) <= ACF_TOL
+    cg, cr = gpu["covmats"], ref["covmats"]
+    fin = np.all(np.isfinite(cr.reshape(len(cr), -1)), axis=1)
+    assert fin.sum() >= 0.8 * len(cr)
+    scale = np.abs(cr[fin]).reshape(fin.sum(), -1).max(axis=1)[:, None, None]
+    assert np.max(np.abs(cg[fin] - cr[fin]) / scale) <= 1e-4
+    np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 0.8 * len(cr)
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+
+
 @pytest.fixture(scope="module")
 def two_species():
     # 70 % of the particles at D = 0.5 um^2/s, 30 % at 5 um^2/s
