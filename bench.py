@@ -367,9 +367,12 @@ def main():
     stack = torch.from_numpy(stack_np.view(np.int16)).cuda().view(torch.uint16)
     torch.cuda.synchronize()
     plan = engine.Plan(cfg)
-    plan.set_timing(True)
     out = plan.alloc_device_outputs()
     stream = torch.cuda.current_stream()
+    # the correlator tile, chosen by the autotuner on this stack (untimed)
+    tile_trials = plan.autotune(stack, out)
+    tile_chosen = dict(zip(("cta", "seg_extra"), plan.corr_tile()))
+    plan.set_timing(True)
 
     def barrier():
         if world > 1:
@@ -483,6 +486,7 @@ def main():
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "gpu_launches": launches,
             "stages_ms": {k: v / args.steps for k, v in stage_acc.items()},
+            "corr_tile": {"chosen": tile_chosen, "trials": tile_trials},
             "roofline": {"kernel": "correlator path: stream_tma (values + monitors), monitor_finalize, block, "
                                    "block_finalize, c2_pair x2, c2_tail, c2_finalize",
                          "bound": "hbm", "achieved": achieved, "peak": peak,

@@ -316,9 +316,9 @@ extern "C" int imfcs_batch_autotune(imfcs_batch *b, const uint16_t *dev_stack, c
             cudaGetLastError();
             break;   // arenas no longer fit: more lanes will not either
         }
-        float t[3] = {0.f, 0.f, 0.f};
+        float t[2] = {0.f, 0.f};
         if (imfcs_batch_execute(b, dev_stack, outs, stream)) { rc = 1; break; }
-        for (int r = 0; r < 3 && !rc; r++) {
+        for (int r = 0; r < 2 && !rc; r++) {
             cudaError_t e = cudaEventRecord(e0, s);
             if (e == cudaSuccess && imfcs_batch_execute(b, dev_stack, outs, stream)) { rc = 1; break; }
             if (e == cudaSuccess) e = cudaEventRecord(e1, s);
@@ -327,9 +327,9 @@ extern "C" int imfcs_batch_autotune(imfcs_batch *b, const uint16_t *dev_stack, c
             if (e != cudaSuccess) { set_error(cuda_msg(e, "batch autotune timing")); rc = 1; }
         }
         if (rc) break;
-        std::sort(t, t + 3);
-        if (lane_ms) lane_ms[nl - 1] = t[1];
-        if (nl == 1 || t[1] < best_t) { best_t = t[1]; best_l = nl; }
+        const float tm = std::min(t[0], t[1]);
+        if (lane_ms) lane_ms[nl - 1] = tm;
+        if (nl == 1 || tm < best_t) { best_t = tm; best_l = nl; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

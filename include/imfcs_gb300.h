@@ -289,7 +289,8 @@ IMFCS_API int imfcs_batch_execute(imfcs_batch *batch, const uint16_t *dev_stack,
 IMFCS_API int imfcs_batch_synchronize(imfcs_batch *batch, void *stream);
 /* Autotuner: tunes every job's correlator tile (imfcs_plan_autotune), times
  * each job alone, then for 1..max_lanes lanes assigns jobs to lanes by
- * longest measured time first and times the whole graph (median of three);
+ * longest measured time first and times the whole graph (best of two after
+ * one warm-up);
  * keeps the fastest lane count.  lane_ms[l-1] receives the time with l lanes
  * (max_lanes entries, 0 where the arenas did not fit in device memory).
  * Synchronises `stream`. */

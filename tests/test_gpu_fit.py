@@ -86,6 +86,31 @@ def test_gls_long_stack_parity(kw):
     assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
 
 
+@pytest.mark.parametrize("gls", [False, True], ids=["ols", "gls"])
+@pytest.mark.parametrize("off", [(1, 0), (1, 1), (0, 2)], ids=["ccf10", "ccf11", "ccf02"])
+def test_ccf_fit_parity(off, gls):
+    """Spatial cross-correlation fits with the window offsets in the model
+    (rx, ry: the three-term lateral factor of FCS_3p, java:13131-13408),
+    OLS and GLS, against the oracle.  Every pixel the oracle fits is fitted
+    with N and D within FIT_TOL.  The weak correlations two pixels apart
+    leave a few fits so flat that the oracle's LM stops at its 2000
+    iterations (not fitted) where the GPU's Newton finish converges: at
+    most 10 % of the pixels are fitted by the GPU alone."""
+    st = brownian_stack(8, 8, 8000, seed=33, density=3.0, cps=3e4)
+    cfx, cfy = off
+    cfg = engine.FCSConfig(width=8, height=8, frames=8000, background=100, cfx=cfx, cfy=cfy, gls=gls,
+                           cst=engine.model_constants(cfx=cfx, cfy=cfy))
+    gpu, ref = run_both(st, cfg)
+    assert acf_deviation(gpu, ref) <= ACF_TOL
+    assert np.all(gpu["fitted"][ref["fitted"] == 1] == 1)
+    assert ((gpu["fitted"] == 1) & (ref["fitted"] == 0)).sum() <= 0.1 * cfg.npix
+    both, errs = fit_errors(gpu, ref)
+    assert both.sum() >= 0.5 * cfg.npix
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+    rel = np.abs(gpu["chi2"][both] / ref["chi2"][both] - 1)
+    assert rel.max() <= 1e-3
+
+
 @pytest.fixture(scope="module")
 def two_species():
     # 70 % of the particles at D = 0.5 um^2/s, 30 % at 5 um^2/s
