@@ -38,6 +38,7 @@ EXPORTS = [
     "imfcs_batch_create", "imfcs_batch_destroy", "imfcs_batch_execute", "imfcs_batch_synchronize",
     "imfcs_batch_autotune", "imfcs_batch_job_info", "imfcs_batch_lanes", "imfcs_batch_scratch_bytes",
     "imfcs_batch_kernel_launches",
+    "imfcs_tiff_open", "imfcs_tiff_read", "imfcs_tiff_read_device", "imfcs_tiff_close", "imfcs_background_stats",
 ]
 
 
@@ -158,6 +159,11 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_batch_scratch_bytes.restype = C.c_size_t
     L.imfcs_batch_scratch_bytes.argtypes = [vp]
     L.imfcs_batch_kernel_launches.argtypes = [vp]
+    L.imfcs_tiff_open.argtypes = [C.c_char_p, C.POINTER(C.c_void_p), ip, ip, ip]
+    L.imfcs_tiff_read.argtypes = [vp, C.c_int, C.c_int, vp]
+    L.imfcs_tiff_read_device.argtypes = [vp, C.c_int, C.c_int, vp, vp]
+    L.imfcs_tiff_close.argtypes = [vp]
+    L.imfcs_background_stats.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

@@ -271,6 +271,30 @@ IMFCS_API int imfcs_plan_get_corr_tile(const imfcs_plan *plan, int *cta, int *se
 IMFCS_API int imfcs_plan_autotune(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,
                         void *stream, imfcs_corr_tile *trials, int max_trials, int *n_trials);
 
+/* Stack ingest (replaces the plugin's ImageJ read, getVoxels
+ * Imaging_FCS_1_52.java:14791 and GPU_get_pixels 14913-14983, which copy
+ * every frame into a Java float array): uncompressed 16-bit single-channel
+ * TIFF stacks in either byte order, one IFD per frame (any strips) or
+ * ImageJ's single-IFD stacks ("images=N" in the description, frames
+ * contiguous).  Frames come out as uint16 [t][height][width] in native
+ * byte order.  imfcs_tiff_read_device copies through two pinned 64 MB
+ * staging buffers used in turn (the file read of a chunk overlaps the
+ * previous chunk's copy) and orders `stream` after the copies. */
+typedef struct imfcs_tiff imfcs_tiff;
+IMFCS_API int imfcs_tiff_open(const char *path, imfcs_tiff **tiff, int *width, int *height, int *frames);
+IMFCS_API int imfcs_tiff_read(imfcs_tiff *tiff, int first, int count, uint16_t *host_out);
+IMFCS_API int imfcs_tiff_read_device(imfcs_tiff *tiff, int first, int count, uint16_t *dev_out, void *stream);
+IMFCS_API int imfcs_tiff_close(imfcs_tiff *tiff);
+
+/* Background-file statistics (loadBGRFile, Imaging_FCS_1_52.java:6988-7103)
+ * of a device-resident background stack dev_stack[frames][height][width]:
+ * per-pixel mean and variance over all frames, lag-1 covariance (means of
+ * frames 1..f-1 and 2..f), row means [height] and column means [width];
+ * device outputs, any may be NULL; identical to the Java's doubles.  The
+ * mean image feeds imfcs_plan_set_background_image.  Asynchronous. */
+IMFCS_API int imfcs_background_stats(const uint16_t *dev_stack, int width, int height, int frames, double *mean,
+                           double *var, double *covar, double *row_mean, double *col_mean, void *stream);
+
 /* Batches (no counterpart in the reference, which repeats one JNI call per
  * binning, Imaging_FCS_1_52.java:11146-11166): several jobs -- binnings,
  * cross-correlation offsets, ROIs of different sizes -- over one stack

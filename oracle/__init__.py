@@ -353,3 +353,25 @@ def run(stack, *, out_w, out_h, map_x0=0, map_y0=0, binx=1, biny=1, pixbinx=None
     if covmats is not None:
         out["covmats"] = covmats
     return out
+
+
+def background_stats(stack):
+    """loadBGRFile (Imaging_FCS_1_52.java:7036-7103) in FP64, in the Java's
+    order: row and column means accumulated frame by frame as
+    line_sum / (len * frames), the lag-1 covariance from the means of frames
+    1..f-1 and 2..f, mean and variance over all frames.  Images are
+    [height][width] (the Java's arrays are [x][y]).  Pixel values, squares and
+    products are integers below 2^53, so every sum is exact."""
+    st = np.asarray(stack).astype(np.float64)
+    f, h, w = st.shape
+    row = np.zeros(h)
+    col = np.zeros(w)
+    for z in range(f):
+        row += st[z].sum(axis=1) / (w * f)
+        col += st[z].sum(axis=0) / (h * f)
+    m1 = st[:-1].sum(axis=0) / (f - 1)
+    m2 = st[1:].sum(axis=0) / (f - 1)
+    covar = (st[:-1] * st[1:]).sum(axis=0) / (f - 1) - m1 * m2
+    mean = st.sum(axis=0) / f
+    var = (st * st).sum(axis=0) / f - mean * mean
+    return {"mean": mean, "var": var, "covar": covar, "row_mean": row, "col_mean": col}
