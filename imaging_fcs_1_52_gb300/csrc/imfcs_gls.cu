@@ -12,20 +12,25 @@
 //
 // One pass over the centred samples e_xz gives, per lag pair (x >= y),
 // S1 = sum_z e_x e_y and S2 = sum_z (e_x e_y)^2 (FP32 per chunk of samples,
-// FP64 across chunks; each thread owns a 4x4 tile of pairs, so a sample
-// loaded from shared memory serves four pairs).  The shrinkage sums follow
+// float-float across chunks; each thread owns a 4x4 tile of pairs, so a
+// sample loaded from shared memory serves four pairs).  The shrinkage sums follow
 // without a second pass:
 //   sum_z (e_x^2 - c_xx)^2               = S2_xx - (pnum - 2) c_xx^2
 //   sum_z (e_x e_y / (sd_x sd_y) - r_xy)^2 = (S2_xy - (pnum - 2) c_xy^2) / (c_xx c_yy)
 // with c = S1 / (pnum - 1) and r = c / (sd_x sd_y).  Divisions by per-lag
 // quantities are multiplications by their reciprocals; the median is a
-// parallel rank selection; the Cholesky updates, L^-1 (one column per
-// thread) and L^-1 mcov (one row per thread) run in FP64 on the packed lower
-// triangle in shared memory.
+// parallel rank selection; the FP64 Cholesky's updates spread over the whole
+// CTA on the packed lower triangle in shared memory.  GB300 issues FP64 at
+// 1/64 of the FP32 rate, so what needs more than FP32 but not the
+// spec FP64 Cholesky -- the centred samples, the sums across chunks,
+// L^-1 (one column per thread) and L^-1 mcov -- runs in float-float
+// (compensated products and sums, about 44 bits) on the FP32 pipe; L^-1
+// leaves the kernel as FP32.
 #include <math.h>
 
 #include "imfcs_internal.cuh"
 #include "imfcs_args.h"
+#include "imfcs_ff.cuh"
 
 namespace imfcs {
 
@@ -37,17 +42,35 @@ constexpr int kGlsTile = 4;                     // pairs per thread: 4 x 4
 
 __device__ __forceinline__ int tri(int r, int c) { return r * (r + 1) / 2 + c; }   // c <= r
 
+// Compensated dot-product step (float-float operands a, b; sum (sh, sl)):
+// the error of the product and of the running sum go to sl, so the result
+// carries about twice the FP32 precision, on the FP32 pipe.  Explicitly
+// rounded operations: a contracted sh + ah*bh would break the two-sum.
+__device__ __forceinline__ void ff_dot_step(float ah, float al, float bh, float bl, float &sh, float &sl)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float pe = __fadd_rn(fmaf(ah, bh, -p), fmaf(ah, bl, __fmul_rn(al, bh)));
+    const float t = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(t, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    sl = __fadd_rn(sl, __fadd_rn(e, pe));
+    sh = t;
+}
+
 __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
 {
     extern __shared__ double gsh[];
     const int n1 = g.chanum - 1;
     const int npairs = n1 * (n1 + 1) / 2;
     const int nrt = (n1 + kGlsTile - 1) / kGlsTile;    // tile rows
-    double *lp = gsh;                  // [npairs] S1 -> covariance/correlation -> regularised -> Cholesky factor
+    double *lp = gsh;                  // [npairs] covariance/correlation -> regularised -> Cholesky factor
     double *s2 = gsh + npairs;         // [npairs] S2 -> t_xy
+    float2 *a1s = (float2 *)lp, *a2s = (float2 *)s2;   // S1, S2 in float-float during the sample pass
     float *eb = (float *)(gsh + 2 * npairs);   // [nrt*4][kGlsZStride] one chunk of centred samples
-    double *xinv = gsh + 2 * npairs;           // [npairs] L^-1 (after the sample passes)
+    float *lh = eb, *ll = eb + npairs;         // L in float-float (after the Cholesky)
+    float *xh = (float *)s2, *xl = xh + npairs;   // L^-1 in float-float
     __shared__ double mcov[kMaxN1], inv_dm[kMaxN1], cdiag[kMaxN1], isd[kMaxN1], sq[kMaxN1], rdiag[kMaxN1];
+    __shared__ f2 inv_dmf[kMaxN1], mcovf[kMaxN1], rdf[kMaxN1];
     __shared__ double red[2][kGlsThreads / 32];
     __shared__ double s_med[2], s_lamvar, s_lamcov, s_piv;
     __shared__ int s_fail;
@@ -60,20 +83,33 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
     if (tid < n1) {
         const float4 m = g.mon[(size_t)pix * g.chanum + tid + 1];
         inv_dm[tid] = 1.0 / ((double)m.z * (double)m.w);
+        inv_dmf[tid] = f2_from_d(inv_dm[tid]);
     }
     if (tid == 0) s_fail = 0;
     for (int i = tid; i < npairs; i += kGlsThreads) { lp[i] = 0.0; s2[i] = 0.0; }
     // rows past n1 of the staging buffer stay zero
     for (int i = n1 * kGlsZStride + tid; i < nrt * kGlsTile * kGlsZStride; i += kGlsThreads) eb[i] = 0.f;
-    // mcov (java:9526-9531): sum of the blocked products, one warp per lag
+    // mcov (java:9526-9531): sum of the blocked products (float-float per
+    // lane and across the warp), one warp per lag
     for (int x = warp; x < n1; x += kGlsThreads / 32) {
-        double sum = 0.0;
-        for (int z = lane; z < pnum; z += 32) sum += (double)bp[(size_t)x * g.pnum_stride + z];
-        sum = warp_sum_d(sum);
-        if (lane == 0) mcov[x] = sum;
+        float sh = 0.f, sl = 0.f;
+        for (int z = lane; z < pnum; z += 32) {
+            const f2 t = f2_two_sum(sh, bp[(size_t)x * g.pnum_stride + z]);
+            sh = t.hi;
+            sl = __fadd_rn(sl, t.lo);
+        }
+        f2 sum = f2_two_sum(sh, sl);
+        for (int o = 16; o > 0; o >>= 1) {
+            const f2 other = {__shfl_xor_sync(0xffffffffu, sum.hi, o), __shfl_xor_sync(0xffffffffu, sum.lo, o)};
+            sum = f2_add(sum, other);
+        }
+        if (lane == 0) mcov[x] = (double)sum.hi + (double)sum.lo;
     }
-    __syncthreads();
-    if (tid < n1) mcov[tid] = mcov[tid] * inv_dm[tid] * inv_pnum;
+    __syncthreads();                  // inv_dm (threads < n1) and the sums (warps)
+    if (tid < n1) {
+        mcov[tid] = mcov[tid] * inv_dm[tid] * inv_pnum;
+        mcovf[tid] = f2_from_d(mcov[tid]);
+    }
     __syncthreads();
 
     // S1, S2 per pair: thread t owns tile (bx, by), bx >= by, of the pairs
@@ -91,11 +127,17 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
         for (int z0 = 0; z0 < pnum; z0 += kGlsZChunk) {
             const int zn = min(kGlsZChunk, pnum - z0);
             __syncthreads();
+            // centred sample e = b / (dm Dm) - mcov in float-float: the
+            // product exactly as hi + lo, then the subtraction of the mean
             for (int i = tid; i < n1 * kGlsZChunk; i += kGlsThreads) {
                 const int x = i / kGlsZChunk, z = i - x * kGlsZChunk;
-                if (z < zn)
-                    eb[x * kGlsZStride + z] =
-                        (float)((double)bp[(size_t)x * g.pnum_stride + z0 + z] * inv_dm[x] - mcov[x]);
+                if (z < zn) {
+                    const float b = bp[(size_t)x * g.pnum_stride + z0 + z];
+                    const f2 iv = inv_dmf[x], mc = mcovf[x];
+                    const float ph = __fmul_rn(b, iv.hi);
+                    const float pl = fmaf(b, iv.lo, fmaf(b, iv.hi, -ph));
+                    eb[x * kGlsZStride + z] = __fadd_rn(__fsub_rn(ph, mc.hi), __fsub_rn(pl, mc.lo));
+                }
             }
             __syncthreads();
             if (t >= ntiles) continue;
@@ -124,15 +166,23 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
                 for (int j = 0; j < kGlsTile; j++) {
                     const int x = kGlsTile * bx + i, y = kGlsTile * by + j;
                     if (x < n1 && y <= x) {
-                        lp[tri(x, y)] += (double)a1[i][j];
-                        s2[tri(x, y)] += (double)a2[i][j];
+                        float2 v = a1s[tri(x, y)];
+                        f2 sv = f2_two_sum(v.x, a1[i][j]);
+                        a1s[tri(x, y)] = make_float2(sv.hi, __fadd_rn(v.y, sv.lo));
+                        v = a2s[tri(x, y)];
+                        sv = f2_two_sum(v.x, a2[i][j]);
+                        a2s[tri(x, y)] = make_float2(sv.hi, __fadd_rn(v.y, sv.lo));
                     }
                 }
         }
     }
     __syncthreads();
-    // covariance (java:9534-9542), standard deviations
-    for (int i = tid; i < npairs; i += kGlsThreads) lp[i] *= inv_pm1;
+    // covariance (java:9534-9542), S2 in FP64, standard deviations
+    for (int i = tid; i < npairs; i += kGlsThreads) {
+        const float2 v = a1s[i], w = a2s[i];
+        lp[i] = ((double)v.x + (double)v.y) * inv_pm1;
+        s2[i] = (double)w.x + (double)w.y;
+    }
     __syncthreads();
     if (tid < n1) {
         const double c = lp[tri(tid, tid)];
@@ -242,26 +292,44 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
             g.covmats_out[(size_t)pix * n1 * n1 + i] = x >= y ? lp[tri(x, y)] : lp[tri(y, x)];
         }
     // Cholesky in commons-math's order (java:13717): pivot i, scale its
-    // column, then the trailing update A[q][p] -= A[q][i] A[p][i] (p <= q)
+    // column, then the trailing update A[q][p] -= A[q][i] A[p][i] (p <= q),
+    // FP64.  The pivot's 1/sqrt by Newton-Raphson from an FP32 estimate
+    // (two steps: ~1e-16), sqrt(d) = d / sqrt(d) corrected once; the update
+    // spreads its (q, p) over the whole CTA.
     for (int i = 0; i < n1; i++) {
         if (tid == 0) {
             const double d = lp[tri(i, i)];
             if (!(d > 1e-10)) {
                 s_fail = 1;
             } else {
-                const double r = sqrt(d);
+                double rs, r;
+                if (d < 1e30) {
+                    rs = (double)rsqrtf((float)d);
+                    rs = rs * fma(-0.5 * d * rs, rs, 1.5);
+                    rs = rs * fma(-0.5 * d * rs, rs, 1.5);
+                    r = d * rs;
+                    r = fma(0.5 * rs, fma(-r, r, d), r);
+                } else {
+                    r = sqrt(d);
+                    rs = 1.0 / r;
+                }
                 lp[tri(i, i)] = r;
-                s_piv = 1.0 / r;
+                s_piv = rs;
+                rdiag[i] = rs;
             }
         }
         __syncthreads();
         if (s_fail) break;
         for (int q = i + 1 + tid; q < n1; q += kGlsThreads) lp[tri(q, i)] *= s_piv;
         __syncthreads();
-        for (int q = i + 1 + warp; q < n1; q += kGlsThreads / 32) {
-            const double aq = lp[tri(q, i)];
-            double *row = lp + tri(q, 0);
-            for (int p = i + 1 + lane; p <= q; p += 32) row[p] -= aq * lp[tri(p, i)];
+        const int m = n1 - 1 - i;
+        const int cnt = m * (m + 1) / 2;
+        for (int e = tid; e < cnt; e += kGlsThreads) {
+            int a = (int)((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
+            while ((a + 1) * (a + 2) / 2 <= e) a++;
+            while (a * (a + 1) / 2 > e) a--;
+            const int q = i + 1 + a, pp = i + 1 + (e - a * (a + 1) / 2);
+            lp[tri(q, pp)] -= lp[tri(q, i)] * lp[tri(pp, i)];
         }
         __syncthreads();
     }
@@ -269,30 +337,44 @@ __global__ void __launch_bounds__(kGlsThreads) gls_kernel(GlsArgs g)
         if (tid == 0) g.ok[pix] = 0;
         return;
     }
-    if (tid < n1) rdiag[tid] = 1.0 / lp[tri(tid, tid)];
+    // L and 1/diag(L) in float-float for the triangular inverse on the FP32
+    // pipe (the output L^-1 is FP32)
+    for (int i = tid; i < npairs; i += kGlsThreads) {
+        const double v = lp[i];
+        const float hi = (float)v;
+        lh[i] = hi;
+        ll[i] = (float)(v - (double)hi);
+    }
+    if (tid < n1) rdf[tid] = f2_from_d(rdiag[tid]);
     __syncthreads();
     // L^-1, column c on thread c: X[c][c] = 1/L[c][c],
     // X[r][c] = -(sum_{m=c}^{r-1} L[r][m] X[m][c]) / L[r][r]
     if (tid < n1) {
         const int c = tid;
-        xinv[tri(c, c)] = rdiag[c];
+        xh[tri(c, c)] = rdf[c].hi;
+        xl[tri(c, c)] = rdf[c].lo;
         for (int r = c + 1; r < n1; r++) {
-            const double *lr = lp + tri(r, 0);
-            double sum = 0.0;
-            for (int m = c; m < r; m++) sum = fma(lr[m], xinv[tri(m, c)], sum);
-            xinv[tri(r, c)] = -sum * rdiag[r];
+            const int rb = tri(r, 0);
+            float sh = 0.f, sl = 0.f;
+            int xi = tri(c, c);
+            for (int m = c; m < r; m++) {
+                ff_dot_step(lh[rb + m], ll[rb + m], xh[xi], xl[xi], sh, sl);
+                xi += m + 1;
+            }
+            const f2 x = f2_mul(f2_two_sum(sh, sl), rdf[r]);
+            xh[tri(r, c)] = -x.hi;
+            xl[tri(r, c)] = -x.lo;
         }
     }
     __syncthreads();
     float *lo = g.linv + (size_t)pix * npairs;
-    for (int i = tid; i < npairs; i += kGlsThreads) lo[i] = (float)xinv[i];
+    for (int i = tid; i < npairs; i += kGlsThreads) lo[i] = __fadd_rn(xh[i], xl[i]);
     // transformed data L^-1 mcov
     if (tid < n1) {
-        const int r = tid;
-        const double *xr = xinv + tri(r, 0);
-        double sum = 0.0;
-        for (int c = 0; c <= r; c++) sum = fma(xr[c], mcov[c], sum);
-        g.ytrans[(size_t)pix * n1 + r] = (float)sum;
+        const int r = tid, rb = tri(r, 0);
+        float sh = 0.f, sl = 0.f;
+        for (int c = 0; c <= r; c++) ff_dot_step(xh[rb + c], xl[rb + c], mcovf[c].hi, mcovf[c].lo, sh, sl);
+        g.ytrans[(size_t)pix * n1 + r] = sh + sl;
     }
     if (tid == 0) g.ok[pix] = 1;
 }

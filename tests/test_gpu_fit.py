@@ -86,6 +86,28 @@ def test_gls_long_stack_parity(kw):
     assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
 
 
+def test_gls_covariance_many_ctas_matches_oracle():
+    """A 96 x 4 strip of a two-component 20,000-frame stack: 384 pixels (a
+    CTA each) with blocking indices 7..10, so the blocked products per lag
+    (pnum) vary between neighbouring CTAs -- the covariance, its shrinkage
+    and the whitened fit against the oracle on every pixel."""
+    import torch
+    full = engine.simulate(128, 16, 20000, d1=0.5, d2=5.0, fraction2=0.3, seed=3)
+    st = engine.to_numpy_u16(full[:, :4, :96].contiguous())
+    torch.cuda.synchronize()
+    cfg = engine.batch_configs(96, 4, 20000, binnings=(1,), offsets=((0, 0),), background=100, gls=True)[0]
+    gpu, ref = run_both(st, cfg)
+    assert len(set(gpu["blocked_ind"].tolist())) >= 2
+    cg, cr = gpu["covmats"], ref["covmats"]
+    fin = np.all(np.isfinite(cr.reshape(len(cr), -1)), axis=1)
+    assert fin.sum() >= 0.9 * len(cr)
+    scale = np.abs(cr[fin]).reshape(fin.sum(), -1).max(axis=1)[:, None, None]
+    assert np.max(np.abs(cg[fin] - cr[fin]) / scale) <= 1e-4
+    np.testing.assert_array_equal(gpu["fitted"], ref["fitted"])
+    both, errs = fit_errors(gpu, ref)
+    assert errs[0].max() <= FIT_TOL and errs[1].max() <= FIT_TOL
+
+
 @pytest.mark.parametrize("off,gls", [((1, 0), False), ((1, 1), False), ((0, 2), False), ((1, 0), True),
                                      ((1, 1), True)],
                          ids=["ccf10-ols", "ccf11-ols", "ccf02-ols", "ccf10-gls", "ccf11-gls"])
