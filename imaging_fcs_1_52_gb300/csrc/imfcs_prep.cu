@@ -812,45 +812,54 @@ __global__ void __launch_bounds__(128) block_kernel(Job j, const float *s0a, con
     segsum[(size_t)seg * j.npix + pix] = segv;     // used only for complete segments
 }
 
-// Blocking decision, one thread per pixel: the segments' statistics
-// combined in FP64 (coalesced across pixels), the levels above the segment
-// size built from segment sums, then the overlap / monotonic-increase
-// criteria of java:9339-9380.
-__global__ void block_finalize_kernel(Job j, int q, int nbseg, const float *s1, const float *s2,
-                                      const float *segsum, const float4 *blkmon, int *ind_out,
-                                      int *ok_out)
+// Blocking decision.  A CTA serves 32 pixels with 8 threads each: thread
+// (pixel, t) sums the segments' statistics of levels t, t + 8, ... in FP64
+// (coalesced across pixels; each level's sum in segment order), the levels
+// above the segment size from segment sums; then one thread per pixel
+// applies the overlap / monotonic-increase criteria of java:9339-9380.
+constexpr int kBlkFinPix = 32, kBlkFinLev = 8;
+__global__ void __launch_bounds__(kBlkFinPix * kBlkFinLev)
+block_finalize_kernel(Job j, int q, int nbseg, const float *s1, const float *s2, const float *segsum,
+                      const float4 *blkmon, int *ind_out, int *ok_out)
 {
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= j.npix) return;
+    __shared__ double S1s[kMaxBlockLevels][kBlkFinPix], S2s[kMaxBlockLevels][kBlkFinPix];
+    const int pl = threadIdx.x % kBlkFinPix, ty = threadIdx.x / kBlkFinPix;
+    const int pix = blockIdx.x * kBlkFinPix + pl;
     const int blocknum = j.blocknum;
-    double S1[kMaxBlockLevels], S2[kMaxBlockLevels];
-    for (int y = 0; y <= kBlkSegLog && y < blocknum; y++) {
-        double a1 = 0.0, a2 = 0.0;
-        const float *p1 = s1 + (size_t)y * nbseg * j.npix + pix, *p2 = s2 + (size_t)y * nbseg * j.npix + pix;
-        for (int seg = 0; seg < nbseg; seg++) {
-            a1 += (double)__ldg(&p1[(size_t)seg * j.npix]);
-            a2 += (double)__ldg(&p2[(size_t)seg * j.npix]);
-        }
-        S1[y] = a1;
-        S2[y] = a2;
-    }
-    // levels above the segment: block y spans 2^(y-8) consecutive complete
-    // segments (a non-finite segment sum, from a non-finite frame, propagates
-    // like the Java sums)
     const int full_segs = (j.num - 1) / kBlkSeg;   // segments holding kBlkSeg products
-    for (int y = kBlkSegLog + 1; y < blocknum; y++) {
-        const int span = 1 << (y - kBlkSegLog);
-        const double inv = 1.0 / (double)(1 << y);
-        double a1 = 0.0, a2 = 0.0;
-        for (int b = 0; (b + 1) * span <= full_segs; b++) {
-            double sb = 0.0;
-            for (int k = 0; k < span; k++) sb += (double)__ldg(&segsum[(size_t)(b * span + k) * j.npix + pix]);
-            const double m = sb * inv;
-            a1 += m;
-            a2 += m * m;
+    if (pix < j.npix) {
+        for (int y = ty; y < blocknum; y += kBlkFinLev) {
+            double a1 = 0.0, a2 = 0.0;
+            if (y <= kBlkSegLog) {
+                const float *p1 = s1 + (size_t)y * nbseg * j.npix + pix, *p2 = s2 + (size_t)y * nbseg * j.npix + pix;
+                for (int seg = 0; seg < nbseg; seg++) {
+                    a1 += (double)__ldg(&p1[(size_t)seg * j.npix]);
+                    a2 += (double)__ldg(&p2[(size_t)seg * j.npix]);
+                }
+            } else {
+                // levels above the segment: block y spans 2^(y-8) consecutive
+                // complete segments (a non-finite segment sum, from a
+                // non-finite frame, propagates like the Java sums)
+                const int span = 1 << (y - kBlkSegLog);
+                const double inv = 1.0 / (double)(1 << y);
+                for (int b = 0; (b + 1) * span <= full_segs; b++) {
+                    double sb = 0.0;
+                    for (int k = 0; k < span; k++) sb += (double)__ldg(&segsum[(size_t)(b * span + k) * j.npix + pix]);
+                    const double m = sb * inv;
+                    a1 += m;
+                    a2 += m * m;
+                }
+            }
+            S1s[y][pl] = a1;
+            S2s[y][pl] = a2;
         }
-        S1[y] = a1;
-        S2[y] = a2;
+    }
+    __syncthreads();
+    if (ty != 0 || pix >= j.npix) return;
+    double S1[kMaxBlockLevels], S2[kMaxBlockLevels];
+    for (int y = 0; y < blocknum; y++) {
+        S1[y] = S1s[y][pl];
+        S2[y] = S2s[y][pl];
     }
     const float4 bm = blkmon[pix];
     const double dmDm = (double)bm.z * (double)bm.w;
@@ -1014,7 +1023,8 @@ cudaError_t launch_block(const Job &j, const float *s0, const float4 *blkmon, in
     block_kernel<<<grid, 128, 0, s>>>(j, s0, s0b, blkmon, nbseg, s1, s2, segsum);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    block_finalize_kernel<<<(j.npix + 127) / 128, 128, 0, s>>>(j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);
+    block_finalize_kernel<<<(j.npix + kBlkFinPix - 1) / kBlkFinPix, kBlkFinPix * kBlkFinLev, 0, s>>>(
+        j, j.q, nbseg, s1, s2, segsum, blkmon, ind, ok);
     return cudaGetLastError();
 }
 
