@@ -512,8 +512,9 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
         }
     }
     // Phase 1: FP32 Levenberg-Marquardt (FP32 parameters, no FP64 operation)
-    // until the Gauss-Newton step is below 1e-3 sigma + 1e-6 |p| (or no step
-    // lowers chi^2 up to lambda 1e10): inside the region where the Newton
+    // until the Gauss-Newton step is below 1e-3 sigma + 1e-6 |p| (or, with
+    // that step within 0.05 sigma, two steps in a row fail to lower chi^2,
+    // or no step lowers it up to lambda 1e10): inside the region where the Newton
     // phase converges quadratically; FP32 sums over 1000 points cannot
     // resolve much smaller steps anyway.
     float A[K * K], lambda = 1e-3f;
@@ -522,16 +523,19 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
     for (int a = 0; a < K; a++) pf[a] = (float)p[a];
     float chi2f = exp_normal32<K>(y, n, dts, iy, pf, A, gf, lane);
     const bool ok = isfinite(chi2f);
-    int evals = 1;
+    int evals = 1, rejected = 0;
     for (int it_n = 0; ok && it_n < 100; it_n++) {
         float h[K];
         unsigned fix;
+        bool gn_near = false;      // Gauss-Newton step within 0.05 sigma
         if (exp_newton_step32<K>(A, gf, pf, fix, h)) {
             bool conv = true;
+            gn_near = true;
             for (int a = 0; a < K; a++) {
                 if ((fix >> a) & 1) continue;
                 const float sig = rsqrtf(fmaxf(A[a * K + a], 1e-30f));
                 conv = conv && fabsf(h[a]) <= 1e-6f * fabsf(pf[a]) + 1e-3f * sig;
+                gn_near = gn_near && fabsf(h[a]) <= 0.05f * sig;
             }
             if (conv) break;
         }
@@ -551,9 +555,15 @@ __global__ void bleach_exp_kernel(Job j, const float *trace, float *bp_out)
             for (int a = 0; a < K * K; a++) A[a] = An[a];
             chi2f = c2n;
             lambda = fmaxf(lambda * 0.1f, 1e-12f);
+            rejected = 0;
         } else {
+            // two rejected steps in a row while the Gauss-Newton step is
+            // within 0.05 sigma: FP32 chi^2 no longer resolves the descent
+            // this close to the minimum -- the Newton phase takes over
+            // (elsewhere rejections raise the damping as usual)
+            rejected = gn_near ? rejected + 1 : 0;
             lambda *= 10.f;
-            if (lambda > 1e10f) break;
+            if (lambda > 1e10f || rejected >= 2) break;
         }
     }
     for (int a = 0; a < K; a++) p[a] = (double)pf[a];
