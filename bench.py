@@ -324,7 +324,7 @@ def batch_block(steps):
     checked = equal = 0
     for k in (0, len(cfgs) // 2, len(cfgs) - 1):
         p = engine.Plan(cfgs[k])
-        p.set_corr_tile(infos[k]["cta"], infos[k]["seg_extra"])
+        p.set_corr_tile(infos[k]["cta"], infos[k]["seg_extra"], infos[k]["tail_extra"])
         o = p.alloc_device_outputs()
         p.execute(stack, o)
         p.synchronize()
@@ -336,7 +336,7 @@ def batch_block(steps):
         del o
     tiles = {}
     for i in infos:
-        key = f"{i['cta']}x2^{i['seg_extra']}"
+        key = f"{i['cta']}x2^{i['seg_extra']}/2^{i['tail_extra']}"
         tiles[key] = tiles.get(key, 0) + 1
     blk = {"workload": f"{Wb}x{Hb}x{Tb} uint16 (GPU Monte-Carlo, D1 0.5 / D2 5 um^2/s, 70/30); binnings 1-5 x "
                        "offsets {0,1,2}^2 = 45 jobs; GLS covariance + GLS LM fit (N, D, G)",
@@ -371,7 +371,7 @@ def main():
     stream = torch.cuda.current_stream()
     # the correlator tile, chosen by the autotuner on this stack (untimed)
     tile_trials = plan.autotune(stack, out)
-    tile_chosen = dict(zip(("cta", "seg_extra"), plan.corr_tile()))
+    tile_chosen = dict(zip(("cta", "seg_extra", "tail_extra"), plan.corr_tile()))
     plan.set_timing(True)
 
     def barrier():

@@ -80,7 +80,7 @@ class Config(C.Structure):
 
 class CorrTile(C.Structure):
     """imfcs_corr_tile."""
-    _fields_ = [("cta", C.c_int), ("seg_extra", C.c_int), ("ms", C.c_float)]
+    _fields_ = [("cta", C.c_int), ("seg_extra", C.c_int), ("tail_extra", C.c_int), ("ms", C.c_float)]
 
 
 class Outputs(C.Structure):
@@ -146,15 +146,15 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_plan_execute_host_async.argtypes = [vp, vp, C.POINTER(Outputs), vp]
     L.imfcs_plan_synchronize.argtypes = [vp, vp]
     L.imfcs_psf_calibration.argtypes = [C.POINTER(Config), vp, C.c_int, C.c_int, dp, C.c_int, C.c_double, dp, vp]
-    L.imfcs_plan_set_corr_tile.argtypes = [vp, C.c_int, C.c_int]
-    L.imfcs_plan_get_corr_tile.argtypes = [vp, ip, ip]
+    L.imfcs_plan_set_corr_tile.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.imfcs_plan_get_corr_tile.argtypes = [vp, ip, ip, ip]
     L.imfcs_plan_autotune.argtypes = [vp, vp, C.POINTER(Outputs), vp, C.POINTER(CorrTile), C.c_int, ip]
     L.imfcs_batch_create.argtypes = [C.POINTER(Config), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
     L.imfcs_batch_destroy.argtypes = [vp]
     L.imfcs_batch_execute.argtypes = [vp, vp, C.POINTER(Outputs), vp]
     L.imfcs_batch_synchronize.argtypes = [vp, vp]
     L.imfcs_batch_autotune.argtypes = [vp, vp, C.POINTER(Outputs), vp, C.c_int, C.POINTER(C.c_float)]
-    L.imfcs_batch_job_info.argtypes = [vp, C.c_int, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
+    L.imfcs_batch_job_info.argtypes = [vp, C.c_int, ip, ip, ip, ip, ip, ip, C.POINTER(C.c_float)]
     L.imfcs_batch_lanes.argtypes = [vp]
     L.imfcs_batch_scratch_bytes.restype = C.c_size_t
     L.imfcs_batch_scratch_bytes.argtypes = [vp]

@@ -338,17 +338,18 @@ extern "C" int imfcs_batch_autotune(imfcs_batch *b, const uint16_t *dev_stack, c
 }
 
 extern "C" int imfcs_batch_job_info(const imfcs_batch *b, int job, int *npix, int *chanum, int *lane, int *cta,
-                                    int *seg_extra, float *ms)
+                                    int *seg_extra, int *tail_extra, float *ms)
 {
     if (!b || job < 0 || job >= (int)b->plans.size()) { set_error("invalid batch job"); return 1; }
     const Job &j = plan_job(b->plans[job]);
     if (npix) *npix = j.npix;
     if (chanum) *chanum = j.chanum;
     if (lane) *lane = b->lane_of[job];
-    int c = 64, x = 0;
-    imfcs_plan_get_corr_tile(b->plans[job], &c, &x);
+    int c = 64, x = 0, tx = 0;
+    imfcs_plan_get_corr_tile(b->plans[job], &c, &x, &tx);
     if (cta) *cta = c;
     if (seg_extra) *seg_extra = x;
+    if (tail_extra) *tail_extra = tx;
     if (ms) *ms = b->job_ms[job];
     return 0;
 }

@@ -1254,23 +1254,25 @@ int plan_corr_only(imfcs_plan *pl, const void *dev_stack, const imfcs_outputs *d
 }
 }  // namespace imfcs
 
-extern "C" int imfcs_plan_set_corr_tile(imfcs_plan *pl, int cta, int seg_extra)
+extern "C" int imfcs_plan_set_corr_tile(imfcs_plan *pl, int cta, int seg_extra, int tail_extra)
 {
     if (!pl) { set_error("null plan"); return 1; }
-    if ((cta != 32 && cta != 64) || seg_extra < 0 || seg_extra > 2) {
-        set_error("correlator tile: cta must be 32 or 64 and seg_extra 0..2");
+    if ((cta != 32 && cta != 64) || seg_extra < 0 || seg_extra > 2 || tail_extra < 0 || tail_extra > 4) {
+        set_error("correlator tile: cta must be 32 or 64, seg_extra 0..2 and tail_extra 0..4");
         return 1;
     }
     pl->job.c2_cta = cta;
     pl->job.c2_seg_extra = seg_extra;
+    pl->job.c2_tail_extra = tail_extra;
     return 0;
 }
 
-extern "C" int imfcs_plan_get_corr_tile(const imfcs_plan *pl, int *cta, int *seg_extra)
+extern "C" int imfcs_plan_get_corr_tile(const imfcs_plan *pl, int *cta, int *seg_extra, int *tail_extra)
 {
-    if (!pl || !cta || !seg_extra) { set_error("null argument"); return 1; }
+    if (!pl || !cta || !seg_extra || !tail_extra) { set_error("null argument"); return 1; }
     *cta = pl->job.c2_cta ? pl->job.c2_cta : 64;
     *seg_extra = pl->job.c2_seg_extra;
+    *tail_extra = pl->job.c2_tail_extra;
     return 0;
 }
 
@@ -1290,35 +1292,51 @@ extern "C" int imfcs_plan_autotune(imfcs_plan *pl, const uint16_t *dev_stack, co
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
+    int n = 0;
+    // median of three launches after one warm-up, of the correlator alone
+    auto trial = [&](int cta, int extra, int tail, float &ms) -> int {
+        pl->job.c2_cta = cta;
+        pl->job.c2_seg_extra = extra;
+        pl->job.c2_tail_extra = tail;
+        if (plan_corr_only(pl, dev_stack, dev_out, s)) return 1;
+        float t[3];
+        for (int r = 0; r < 3; r++) {
+            cudaError_t e = cudaEventRecord(e0, s);
+            if (e == cudaSuccess && plan_corr_only(pl, dev_stack, dev_out, s)) return 1;
+            if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], e0, e1);
+            if (e != cudaSuccess) { set_error(cuda_msg(e, "autotune timing")); return 1; }
+        }
+        std::sort(t, t + 3);
+        ms = t[1];
+        if (trials && n < max_trials) trials[n] = {cta, extra, tail, ms};
+        n++;
+        return 0;
+    };
+    // pixels per CTA x the pair kernels' segment (tail segment alike), then
+    // the tail kernel's segment alone
     const int ctas[2] = {64, 32};
-    const int extras[3] = {0, 1, 2};
     float best = 0.f;
-    int best_cta = 64, best_extra = 0, n = 0;
+    int best_cta = 64, best_extra = 0, best_tail = 0;
     for (int ci = 0; ci < 2 && !rc; ci++)
         for (int xi = 0; xi < 3 && !rc; xi++) {
-            pl->job.c2_cta = ctas[ci];
-            pl->job.c2_seg_extra = extras[xi];
-            // warm-up, then the median of three launches
-            if (plan_corr_only(pl, dev_stack, dev_out, s)) { rc = 1; break; }
-            float t[3];
-            for (int r = 0; r < 3 && !rc; r++) {
-                cudaError_t e = cudaEventRecord(e0, s);
-                if (e == cudaSuccess && plan_corr_only(pl, dev_stack, dev_out, s)) { rc = 1; break; }
-                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&t[r], e0, e1);
-                if (e != cudaSuccess) { set_error(cuda_msg(e, "autotune timing")); rc = 1; }
-            }
-            if (rc) break;
-            std::sort(t, t + 3);
-            if (trials && n < max_trials) trials[n] = {ctas[ci], extras[xi], t[1]};
-            n++;
-            if (n == 1 || t[1] < best) { best = t[1]; best_cta = ctas[ci]; best_extra = extras[xi]; }
+            float ms = 0.f;
+            if (trial(ctas[ci], xi, xi, ms)) { rc = 1; break; }
+            if (n == 1 || ms < best) { best = ms; best_cta = ctas[ci]; best_extra = xi; best_tail = xi; }
         }
+    const int pair_extra = best_extra;
+    for (int ti = 0; ti <= 4 && !rc; ti++) {
+        if (ti == pair_extra) continue;
+        float ms = 0.f;
+        if (trial(best_cta, best_extra, ti, ms)) { rc = 1; break; }
+        if (ms < best) { best = ms; best_tail = ti; }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     pl->job.c2_cta = best_cta;
     pl->job.c2_seg_extra = best_extra;
+    pl->job.c2_tail_extra = best_tail;
     if (n_trials) *n_trials = n < max_trials ? n : max_trials;
     return rc;
 }

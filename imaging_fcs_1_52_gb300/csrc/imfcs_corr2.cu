@@ -34,7 +34,7 @@
 namespace imfcs {
 
 constexpr int kC2Threads = 64;       // pixels per CTA unless the tile says 32
-constexpr int kMaxSegExtra = 3;
+constexpr int kMaxSegExtra = 4;
 constexpr int kHeadFields = (kP + 1) + 8;                   // first-level heads d = 0..16, second-level d = 9..16
 
 // Arguments shared by the pair, tail and finalise kernels.
@@ -786,9 +786,12 @@ struct Plan2 {
 Plan2 plan2(const Job &j)
 {
     Plan2 p;
-    // every pixel's block length divides 2^base frames; the tile's segment
-    // extension multiplies every segment by 2^c2_seg_extra
-    const int base = max(j.blocknum - 1, j.q - 1) + min(max(j.c2_seg_extra, 0), kMaxSegExtra);
+    // every pixel's block length divides 2^base0 frames; the tile multiplies
+    // the pair kernels' segments by 2^c2_seg_extra and the tail kernel's by
+    // 2^c2_tail_extra
+    const int base0 = max(j.blocknum - 1, j.q - 1);
+    const int base = base0 + min(max(j.c2_seg_extra, 0), kMaxSegExtra);
+    const int base_tail = base0 + min(max(j.c2_tail_extra, 0), kMaxSegExtra);
     p.npair = (j.q >= 7) ? 2 : 1;
     p.k_tail = 2 * p.npair;
     for (int k = 0; k < kMaxLevels; k++) p.seg_log[k] = 0;
@@ -798,7 +801,7 @@ Plan2 plan2(const Job &j)
         p.seg_log[k] = p.seg_log[k + 1] = sl;
     }
     if (p.k_tail < j.q) {
-        const int sl = max(base, p.k_tail);
+        const int sl = max(base_tail, p.k_tail);
         for (int k = p.k_tail; k < j.q; k++) p.seg_log[k] = sl;
     }
     p.nseg_max = 1;

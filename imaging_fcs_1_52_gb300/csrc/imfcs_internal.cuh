@@ -58,9 +58,10 @@ struct Job {
     // lag tables (device copies live in constant memory per launch via Job)
     int nsnap;
     // correlator tile of the level chain (chosen by the autotuner): pixels
-    // per CTA (32 or 64; 0 = 64) and frame segments 2^c2_seg_extra times the
+    // per CTA (32 or 64; 0 = 64) and frame segments of the pair kernels and
+    // of the tail kernel, 2^c2_seg_extra and 2^c2_tail_extra times the
     // shortest legal segment
-    int c2_cta, c2_seg_extra;
+    int c2_cta, c2_seg_extra, c2_tail_extra;
 };
 
 // Lag tables, snapshot positions and per-lag snapshot indices, stored in a

@@ -274,15 +274,19 @@ class Plan:
         sp = None if stream is None else C.c_void_p(stream.cuda_stream)
         check(self._L.imfcs_plan_synchronize(self._h, sp), "imfcs_plan_synchronize")
 
-    def set_corr_tile(self, cta: int, seg_extra: int):
+    def set_corr_tile(self, cta: int, seg_extra: int, tail_extra: int | None = None):
         """Correlator tile of the level chain: cta pixels per CTA (32 or 64),
-        frame segments 2^seg_extra times the shortest legal one."""
-        check(self._L.imfcs_plan_set_corr_tile(self._h, int(cta), int(seg_extra)), "imfcs_plan_set_corr_tile")
+        the pair kernels' frame segments 2^seg_extra and the tail kernel's
+        2^tail_extra (default: seg_extra) times the shortest legal one."""
+        t = seg_extra if tail_extra is None else tail_extra
+        check(self._L.imfcs_plan_set_corr_tile(self._h, int(cta), int(seg_extra), int(t)),
+              "imfcs_plan_set_corr_tile")
 
-    def corr_tile(self) -> tuple[int, int]:
-        a, b = C.c_int(), C.c_int()
-        check(self._L.imfcs_plan_get_corr_tile(self._h, C.byref(a), C.byref(b)), "imfcs_plan_get_corr_tile")
-        return int(a.value), int(b.value)
+    def corr_tile(self) -> tuple[int, int, int]:
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(self._L.imfcs_plan_get_corr_tile(self._h, C.byref(a), C.byref(b), C.byref(c)),
+              "imfcs_plan_get_corr_tile")
+        return int(a.value), int(b.value), int(c.value)
 
     def autotune(self, stack, outputs: dict, stream=None) -> list[dict]:
         """Time the correlator at every tile on this stack, keep the fastest
@@ -294,7 +298,8 @@ class Plan:
         n = C.c_int()
         check(self._L.imfcs_plan_autotune(self._h, C.c_void_p(stack.data_ptr()), C.byref(o),
                                           C.c_void_p(s.cuda_stream), trials, 16, C.byref(n)), "imfcs_plan_autotune")
-        return [{"cta": t.cta, "seg_extra": t.seg_extra, "ms": float(t.ms)} for t in trials[:n.value]]
+        return [{"cta": t.cta, "seg_extra": t.seg_extra, "tail_extra": t.tail_extra, "ms": float(t.ms)}
+                for t in trials[:n.value]]
 
 
 def batch_configs(width: int, height: int, frames: int, binnings=(1, 2, 3, 4, 5),
@@ -350,12 +355,12 @@ class Batch:
         return int(self._L.imfcs_batch_kernel_launches(self._h))
 
     def job_info(self, i: int) -> dict:
-        v = [C.c_int() for _ in range(5)]
+        v = [C.c_int() for _ in range(6)]
         ms = C.c_float()
         check(self._L.imfcs_batch_job_info(self._h, i, *[C.byref(x) for x in v], C.byref(ms)),
               "imfcs_batch_job_info")
         return {"npix": v[0].value, "chanum": v[1].value, "lane": v[2].value, "cta": v[3].value,
-                "seg_extra": v[4].value, "ms": float(ms.value)}
+                "seg_extra": v[4].value, "tail_extra": v[5].value, "ms": float(ms.value)}
 
     def alloc_device_outputs(self, device="cuda") -> list[dict]:
         import torch

@@ -254,20 +254,24 @@ IMFCS_API int imfcs_plan_stage_times(const imfcs_plan *plan, float *ms, int max_
 
 /* Correlator tile of the level chain (no counterpart in the reference, whose
  * kernels use fixed 16x16 thread blocks, agpufitjni.cu:5521-5531): `cta`
- * output pixels per CTA (32 or 64) and frame segments 2^seg_extra (0..2)
- * times the shortest legal segment (the block length of the blocked
- * variance).  Results agree to FP32 rounding of the per-segment sums. */
+ * output pixels per CTA (32 or 64), the pair kernels' frame segments
+ * 2^seg_extra (0..2) and the tail kernel's 2^tail_extra (0..4) times the
+ * shortest legal segment (the block length of the blocked variance).
+ * Results agree to FP32 rounding of the per-segment sums. */
 typedef struct imfcs_corr_tile {
     int cta;
     int seg_extra;
+    int tail_extra;
     float ms;                 /* median correlator time of the trial */
 } imfcs_corr_tile;
-IMFCS_API int imfcs_plan_set_corr_tile(imfcs_plan *plan, int cta, int seg_extra);
-IMFCS_API int imfcs_plan_get_corr_tile(const imfcs_plan *plan, int *cta, int *seg_extra);
+IMFCS_API int imfcs_plan_set_corr_tile(imfcs_plan *plan, int cta, int seg_extra, int tail_extra);
+IMFCS_API int imfcs_plan_get_corr_tile(const imfcs_plan *plan, int *cta, int *seg_extra, int *tail_extra);
 /* Autotuner: executes the plan once on dev_stack (outputs as
- * imfcs_plan_execute), then times the correlator at every tile (median of
- * three launches after one warm-up) and keeps the fastest.  Writes up to
- * max_trials trials.  Synchronises `stream`. */
+ * imfcs_plan_execute), then times the correlator (median of three launches
+ * after one warm-up) at the six (cta, seg_extra) tiles with the tail
+ * segment alike, then at the other tail segments of the fastest, and keeps
+ * the fastest (10 trials).  Writes up to max_trials trials.  Synchronises
+ * `stream`. */
 IMFCS_API int imfcs_plan_autotune(imfcs_plan *plan, const uint16_t *dev_stack, const imfcs_outputs *dev_out,
                         void *stream, imfcs_corr_tile *trials, int max_trials, int *n_trials);
 
@@ -323,7 +327,7 @@ IMFCS_API int imfcs_batch_autotune(imfcs_batch *batch, const uint16_t *dev_stack
 /* Per job: output pixels, channels, lane, correlator tile and measured time
  * (ms, 0 before autotuning). */
 IMFCS_API int imfcs_batch_job_info(const imfcs_batch *batch, int job, int *npix, int *chanum, int *lane,
-                         int *cta, int *seg_extra, float *ms);
+                         int *cta, int *seg_extra, int *tail_extra, float *ms);
 IMFCS_API int imfcs_batch_lanes(const imfcs_batch *batch);
 /* Device bytes of the scratch arenas and of the jobs' own tables. */
 IMFCS_API size_t imfcs_batch_scratch_bytes(const imfcs_batch *batch);

@@ -120,7 +120,8 @@ def test_batch_gls_jobs_equal_standalone_plans():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tile", [(64, 0), (64, 1), (64, 2), (32, 0), (32, 1), (32, 2)])
+@pytest.mark.parametrize("tile", [(64, 0, 0), (64, 1, 1), (64, 2, 2), (32, 0, 0), (32, 1, 1), (32, 2, 2),
+                                  (64, 0, 3), (64, 1, 4), (32, 2, 0)])
 @pytest.mark.parametrize("kw", [{}, {"cfx": 1, "cfy": 1}, {"binx": 2, "biny": 2}], ids=["acf", "ccf11", "bin2"])
 def test_corr_tiles_match_oracle(tile, kw):
     import oracle
@@ -150,16 +151,16 @@ def test_plan_autotune_keeps_a_measured_tile():
     try:
         out = plan.alloc_device_outputs()
         trials = plan.autotune(dev, out)
-        assert len(trials) == 6 and all(t["ms"] > 0 for t in trials)
+        assert len(trials) == 10 and all(t["ms"] > 0 for t in trials)
         best = min(trials, key=lambda t: t["ms"])
-        assert plan.corr_tile() == (best["cta"], best["seg_extra"])
+        assert plan.corr_tile() == (best["cta"], best["seg_extra"], best["tail_extra"])
         plan.execute(dev, out)
         plan.synchronize()
         torch.cuda.synchronize()
         got = {k: v.cpu().numpy() for k, v in out.items()}
     finally:
         plan.close()
-    _assert_same(_plan_outputs(cfg, dev, (best["cta"], best["seg_extra"])), got)
+    _assert_same(_plan_outputs(cfg, dev, (best["cta"], best["seg_extra"], best["tail_extra"])), got)
 
 
 @pytest.mark.gpu
@@ -180,7 +181,7 @@ def test_batch_autotune_lanes_and_results():
         batch.synchronize()
         torch.cuda.synchronize()
         for c, i, o in zip(cfgs, infos, outs):
-            _assert_same(_plan_outputs(c, dev, (i["cta"], i["seg_extra"])),
+            _assert_same(_plan_outputs(c, dev, (i["cta"], i["seg_extra"], i["tail_extra"])),
                          {k: v.cpu().numpy() for k, v in o.items()})
     finally:
         batch.close()
