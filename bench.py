@@ -237,7 +237,7 @@ def surrogate_block(plan, stack, steps):
     """Surrogate-seeded LM against plain LM on the same correlator outputs:
     fit-stage device time (features + MLP + seeded LM + refits in the seeded
     mode), fitted pixels/s, and agreement at equal chi^2 (mode 1: refit of
-    failed seeded fits; mode 2: plain LM also runs and judges every pixel)."""
+    failed seeded fits; mode 2: plain LM also runs and arbitrates every pixel)."""
     import torch
     from imaging_fcs_1_52_gb300 import surrogate
     if not os.path.exists(surrogate.DEFAULT_WEIGHTS):

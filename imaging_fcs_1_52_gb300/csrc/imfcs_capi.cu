@@ -657,7 +657,7 @@ static int run_fit(imfcs_plan *pl, cudaStream_t s, const double *acf, const floa
 }
 
 // Surrogate-seeded LM: features + MLP + per-pixel seeds, the seeded LM, the
-// refit decision (and in mode 2 the plain-LM judge), LM from the configured
+// refit decision (and in mode 2 the plain-LM arbiter), LM from the configured
 // initial values on the refit pixels, then the epilogue.
 static int run_fit_seeded(imfcs_plan *pl, cudaStream_t s, const double *acf, const double *var, const float *y,
                           const float *w, float *fitres, float *chi2, int *fitted, int *iters)
@@ -669,8 +669,8 @@ static int run_fit_seeded(imfcs_plan *pl, cudaStream_t s, const double *acf, con
         return 1;
     pl->launches += 7;   // features, BF16 inputs, 3 GEMMs, de-standardise, seeds
     if (pl->sur_mode == 2) {
-        const LMOut judge{pl->plain_par, pl->plain_chi2, nullptr, pl->plain_state, nullptr};
-        if (run_lm(pl, s, y, w, pl->fit_init, 0, pl->k, pl->idx, nullptr, judge)) return 1;
+        const LMOut arbiter{pl->plain_par, pl->plain_chi2, nullptr, pl->plain_state, nullptr};
+        if (run_lm(pl, s, y, w, pl->fit_init, 0, pl->k, pl->idx, nullptr, arbiter)) return 1;
     }
     const LMOut o{pl->fit_par, pl->fit_chi2, pl->fit_hess, pl->fit_state, it_out};
     if (run_lm(pl, s, y, w, pl->sur_init, IMFCS_NPARAM, pl->k, pl->idx, nullptr, o)) return 1;

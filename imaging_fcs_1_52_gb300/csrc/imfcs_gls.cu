@@ -22,7 +22,7 @@
 // parallel rank selection; the FP64 Cholesky's updates spread over the whole
 // CTA on the packed lower triangle in shared memory.  GB300 issues FP64 at
 // 1/64 of the FP32 rate, so what needs more than FP32 but not the
-// spec FP64 Cholesky -- the centred samples, the sums across chunks,
+// FP64 Cholesky -- the centred samples, the sums across chunks,
 // L^-1 (one column per thread) and L^-1 mcov -- runs in float-float
 // (compensated products and sums, about 44 bits) on the FP32 pipe; L^-1
 // leaves the kernel as FP32.

@@ -4,7 +4,7 @@
 // FP32 master weights, and the input features built on the device from the
 // correlator's outputs.  It has no counterpart in the reference, whose fits
 // start from fixed values (N = 1, D = 1 um^2/s, G = 0; Imaging_FCS_1_52.java
-// :1958-1970); plain LM from those values stays the fallback and the judge of
+// :1958-1970); plain LM from those values stays the fallback and the arbiter of
 // the seeded fits.
 //
 // Network: x[128] -> z1 = x W1 + b1 [256] -> h1 = GELU(z1) -> z2 = h1 W2 + b2

@@ -10,7 +10,7 @@ predictions of
 
 and a plan with the surrogate attached (Plan.set_surrogate) starts each
 pixel's LM from them.  Plain LM from the configured initial values stays the
-fallback (failed seeded fits are refit) and, in mode 2, the judge.
+fallback (failed seeded fits are refit) and, in mode 2, the arbiter.
 
 Training data come from the project's own Monte-Carlo simulator
 (imfcs_simulate) and correlator: seeded stacks over log-uniform D, N and

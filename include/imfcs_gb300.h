@@ -453,7 +453,7 @@ IMFCS_API int imfcs_surrogate_predict(imfcs_surrogate *s, const float *dev_x, in
  * mode 2: as mode 1, and plain LM from the configured initial values also
  *         runs for every pixel; a pixel whose seeded chi^2 exceeds the plain
  *         chi^2 by more than 1 % takes the plain result (the plain fit is the
- *         judge of the seeded one).
+ *         arbiter of the seeded one).
  * The plan keeps the pointer; the surrogate must outlive its use. */
 IMFCS_API int imfcs_plan_set_surrogate(imfcs_plan *plan, imfcs_surrogate *s, int mode);
 /* Per-pixel background image, the plugin's background-file mode (bgrloaded:

@@ -1,6 +1,6 @@
 """The learned part: MLP surrogate kernels (BF16 tensor cores, FP32
 accumulation) against torch-CPU FP64 autograd, its training on simulator +
-correlator curves, and surrogate-seeded LM against plain LM (the judge).
+correlator curves, and surrogate-seeded LM against plain LM (the arbiter).
 
 Also the simulator check the training data rest on: correlate + fit of a
 simulated stack recovers the simulated D and N (the semantics of
