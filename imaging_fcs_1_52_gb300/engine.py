@@ -302,6 +302,25 @@ class Plan:
                 for t in trials[:n.value]]
 
 
+def lag_tables(p: int, q: int) -> tuple[np.ndarray, np.ndarray]:
+    """Lag (frames) and bin width of every channel (java:7391-7424): level 0
+    lags 0..p, then p/2 lags per level k = 1..q-1 at bin width 2^k."""
+    hb = p // 2
+    ch = int(p + (q - 1) * p / 2 + 1)
+    lag = np.zeros(ch, np.int64)
+    samp = np.ones(ch)
+    for x in range(hb + 1):
+        lag[x] = x
+    for x in range(1, q + 1):
+        for y in range(1, hb + 1):
+            i = x * hb + y
+            if i < ch:
+                lag[i] = 2 ** (x - 1) * y + (p // 4) * 2 ** x
+                if x >= 2:
+                    samp[i] = 2 ** (x - 1)
+    return lag, samp
+
+
 def batch_configs(width: int, height: int, frames: int, binnings=(1, 2, 3, 4, 5),
                   offsets=((0, 0), (1, 0), (2, 0), (0, 1), (1, 1), (2, 1), (0, 2), (1, 2), (2, 2)),
                   **kw) -> list[FCSConfig]:
