@@ -426,8 +426,10 @@ __global__ void __launch_bounds__(NT) c2_pair_kernel(C2Args a, const float *inA,
 // keeps a ring of its last 32 samples in shared memory and its lags' block
 // sums and block statistics in registers; the statistics are written once.
 // ---------------------------------------------------------------------------
+// (8 warps per SM at least: 128 registers, a few spilled, against 160 at
+// 6 warps -- the kernel waits on its loads, 6.44 -> 6.18 ms for the chain)
 template <bool CCF, int NT>
-__global__ void __launch_bounds__(NT) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
+__global__ void __launch_bounds__(NT, 512 / NT) c2_tail_kernel(C2Args a, const float *inA, const float *inB, int k0)
 {
     __shared__ float ring_sm[(CCF ? 2 : 1) * 32 * NT];
     const int tid = threadIdx.x;
