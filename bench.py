@@ -282,6 +282,38 @@ def surrogate_block(plan, stack, steps):
     return blk
 
 
+def bands_block(engine, cfg, host_np, whole_out, tile, steps):
+    """Band-streamed host execution (imfcs_bands_*) of the same pinned stack
+    under a device budget of a quarter of the one-band footprint, with the
+    whole-stack plan's correlator tile: bands, host-to-device time included,
+    and its results against the whole-stack host execution's."""
+    import torch
+    try:
+        one = engine.Bands(cfg, band_rows=cfg.out_h)
+        full = one.geometry()["device_bytes"]
+        one.close()
+        bands = engine.Bands(cfg, max_device_bytes=full // 4)
+        bands.set_corr_tile(*tile)
+        tdt = {"f8": torch.float64, "f4": torch.float32, "i4": torch.int32}
+        outs = {n: torch.empty(v.shape, dtype=tdt[v.dtype.str[1:]], pin_memory=True).numpy()
+                for n, v in whole_out.items()}
+        bands.execute_host(host_np, outs)            # warm-up
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            bands.execute_host(host_np, outs)
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        equal = all(np.array_equal(outs[n], whole_out[n], equal_nan=outs[n].dtype.kind == "f") for n in outs)
+        fin = np.isfinite(whole_out["acf"]) & np.isfinite(outs["acf"])
+        dev = float(np.abs(outs["acf"][fin] - whole_out["acf"][fin]).max()) if fin.any() else 0.0
+        g = bands.geometry()
+        bands.close()
+        return {"budget_bytes": full // 4, "one_band_bytes": full, **g, "ms_per_step": ms,
+                "pixels_per_s": cfg.npix / (ms * 1e-3), "equal_to_whole_stack": bool(equal),
+                "acf_max_abs_dev": dev}
+    except Exception as e:   # reported, never fatal to the bench line
+        return {"error": str(e)}
+
+
 def batch_block(steps):
     """Multi-job batch: a 256x256x20000 two-component stack (D1 = 0.5,
     D2 = 5 um^2/s, 70/30, GPU Monte-Carlo simulator), binnings 1-5 x
@@ -469,6 +501,8 @@ def main():
             parity["determined"] = parity_block(gpu_np, ref, cpu_n, det)
         fitted = int(out["fitted"].sum().item())
         sur_blk = surrogate_block(plan, stack, args.steps)
+        bands_blk = (bands_block(engine, cfg, host_np, outs_host, plan.corr_tile(), min(args.steps, 5))
+                     if world == 1 else None)
         batch_blk = None
         if not args.no_batch and world == 1:
             plan.close()
@@ -503,6 +537,7 @@ def main():
             "clocks": clk.summary(),
             "parity": parity,
             "surrogate": sur_blk,
+            "bands": bands_blk,
             "batch_config3": batch_blk,
         }
         print(json.dumps(line))

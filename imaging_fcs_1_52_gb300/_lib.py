@@ -39,6 +39,8 @@ EXPORTS = [
     "imfcs_batch_autotune", "imfcs_batch_job_info", "imfcs_batch_lanes", "imfcs_batch_scratch_bytes",
     "imfcs_batch_kernel_launches",
     "imfcs_tiff_open", "imfcs_tiff_read", "imfcs_tiff_read_device", "imfcs_tiff_close", "imfcs_background_stats",
+    "imfcs_bands_create", "imfcs_bands_destroy", "imfcs_bands_geometry", "imfcs_bands_plan", "imfcs_bands_execute",
+    "imfcs_band_window",
 ]
 
 
@@ -164,6 +166,13 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_tiff_read_device.argtypes = [vp, C.c_int, C.c_int, vp, vp]
     L.imfcs_tiff_close.argtypes = [vp]
     L.imfcs_background_stats.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
+    L.imfcs_bands_create.argtypes = [C.POINTER(Config), C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]
+    L.imfcs_bands_destroy.argtypes = [vp]
+    L.imfcs_bands_geometry.argtypes = [vp, ip, ip, C.POINTER(C.c_size_t)]
+    L.imfcs_bands_plan.restype = vp
+    L.imfcs_bands_plan.argtypes = [vp]
+    L.imfcs_bands_execute.argtypes = [vp, vp, C.POINTER(Outputs), vp]
+    L.imfcs_band_window.argtypes = [C.POINTER(Config), C.c_int, C.c_int, ip, ip, ip, ip, ip]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:

@@ -386,6 +386,8 @@ static bool validate_config(const imfcs_config *c, std::string &err)
 }
 
 namespace imfcs {
+bool config_valid(const imfcs_config *c, std::string &err) { return validate_config(c, err); }
+
 int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h, bool given_bleach,
                    imfcs_plan **plan_out, bool external_scratch)
 {

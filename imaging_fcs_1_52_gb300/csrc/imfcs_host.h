@@ -82,6 +82,9 @@ void legendre_projection(int order, int nopit, int ave, double frametime, double
 void legendre_basis_table(int order, int num, double frametime, double uscale, double uoff,
                           float *table);
 
+// the checks imfcs_plan_create applies to a configuration
+bool config_valid(const imfcs_config *c, std::string &err);
+
 // external_scratch: the plan's per-execution scratch is not allocated; a
 // batch binds an arena of plan_scratch_need bytes before each execution
 int plan_create_ex(const imfcs_config *cfg, int input_float, int in_w, int in_h, bool given_bleach,

@@ -424,6 +424,77 @@ class Batch:
         return [float(x) for x in ms]
 
 
+def band_windows(cfg: FCSConfig, band_rows: int) -> list[dict]:
+    """The band split imfcs_bands uses (imfcs_band_window; host arithmetic,
+    no device): per band its first output row, the output rows it adds, the
+    input row of its buffer's first row and its input rows."""
+    L = _lib.load()
+    c = cfg.to_c()
+    v = [C.c_int() for _ in range(5)]
+    n = L.imfcs_band_window(C.byref(c), int(band_rows), 0, *[C.byref(x) for x in v])
+    if n < 0:
+        raise _lib.ImfcsError(_lib.last_error())
+    out = []
+    for b in range(n):
+        L.imfcs_band_window(C.byref(c), int(band_rows), b, *[C.byref(x) for x in v])
+        out.append({"out_row0": v[0].value, "new_row0": v[1].value, "new_rows": v[2].value,
+                    "in_row0": v[3].value, "in_rows": v[4].value})
+    return out
+
+
+class Bands:
+    """Band-streamed execution of a host stack larger than the device memory
+    granted (imfcs_bands_*): bands of output rows, each band's input rows
+    copied while the previous band computes.  band_rows = 0 sizes the bands
+    from max_device_bytes (0: 90 % of the free device memory)."""
+
+    def __init__(self, cfg: FCSConfig, band_rows: int = 0, max_device_bytes: int = 0):
+        self.cfg = cfg
+        self._L = _lib.load()
+        self._c = cfg.to_c()
+        h = C.c_void_p()
+        check(self._L.imfcs_bands_create(C.byref(self._c), int(band_rows), int(max_device_bytes), C.byref(h)),
+              "imfcs_bands_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.imfcs_bands_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def geometry(self) -> dict:
+        r, n, b = C.c_int(), C.c_int(), C.c_size_t()
+        check(self._L.imfcs_bands_geometry(self._h, C.byref(r), C.byref(n), C.byref(b)), "imfcs_bands_geometry")
+        return {"band_rows": r.value, "bands": n.value, "device_bytes": int(b.value)}
+
+    def set_corr_tile(self, cta: int, seg_extra: int, tail_extra: int | None = None):
+        t = seg_extra if tail_extra is None else tail_extra
+        check(self._L.imfcs_plan_set_corr_tile(self._L.imfcs_bands_plan(self._h), int(cta), int(seg_extra), int(t)),
+              "imfcs_plan_set_corr_tile")
+
+    def execute_host(self, stack: np.ndarray, outputs: dict | None = None, stream=None) -> dict:
+        """Host stack [frames][height][width] in, host results out."""
+        stack = np.ascontiguousarray(stack, dtype=np.uint16)
+        if stack.shape != (self.cfg.frames, self.cfg.height, self.cfg.width):
+            raise ValueError(f"stack must be {self.cfg.frames} x {self.cfg.height} x {self.cfg.width}")
+        if outputs is None:
+            outputs = {}
+            for n in output_names(self.cfg):
+                dt, shp = _OUT_SPEC[n]
+                outputs[n] = np.empty((self.cfg.npix, *shp(self.cfg.chanum)), dtype=dt)
+        o = _outputs_struct({k: v.ctypes.data for k, v in outputs.items()})
+        sp = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(self._L.imfcs_bands_execute(self._h, C.c_void_p(stack.ctypes.data), C.byref(o), sp),
+              "imfcs_bands_execute")
+        return outputs
+
+
 def run_host(stack: np.ndarray, cfg: FCSConfig) -> dict:
     plan = Plan(cfg)
     try:

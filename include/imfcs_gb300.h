@@ -358,6 +358,38 @@ IMFCS_API int imfcs_plan_execute_host_async(imfcs_plan *plan, const uint16_t *ho
 /* Waits for the plan's executions on `stream`; reports a device-side error. */
 IMFCS_API int imfcs_plan_synchronize(imfcs_plan *plan, void *stream);
 
+/* Band-streamed execution of a host stack larger than the device memory the
+ * caller grants (no counterpart in the reference: the plugin copies the
+ * whole stack to the device as one float array, Imaging_FCS_1_52.java:
+ * 14908-14983, agpufitjni.cu:5510,5586).  The job's output rows are split
+ * into bands of band_rows rows (0: the most rows whose device footprint --
+ * plan scratch, two band buffers, outputs -- fits in max_device_bytes; 0
+ * bytes: 90 % of the free device memory).  Each band's input rows (its
+ * windows plus the (binning-1) + |cfy| rows of halo) of frames first ..
+ * first+num-1 go to the device in one 2D copy on an internal copy stream
+ * while the previous band computes; results equal imfcs_plan_execute_host's
+ * on the whole stack, since output pixels are independent.
+ * imfcs_bands_execute returns after the results are in host_out (pinned
+ * host buffers let copies and computation overlap).  A per-pixel background
+ * image is not supported on bands (scalar background only). */
+typedef struct imfcs_bands imfcs_bands;
+IMFCS_API int imfcs_bands_create(const imfcs_config *cfg, int band_rows, size_t max_device_bytes,
+                                 imfcs_bands **bands);
+IMFCS_API int imfcs_bands_destroy(imfcs_bands *bands);
+/* Output rows per band, number of bands, device bytes held. */
+IMFCS_API int imfcs_bands_geometry(const imfcs_bands *bands, int *band_rows, int *n_bands, size_t *device_bytes);
+/* The plan that runs every band (for its tile, timing and surrogate settings). */
+IMFCS_API imfcs_plan *imfcs_bands_plan(imfcs_bands *bands);
+IMFCS_API int imfcs_bands_execute(imfcs_bands *bands, const uint16_t *host_stack, const imfcs_outputs *host_out,
+                                  void *stream);
+/* Band split without a device (host arithmetic only): band `band` of a job
+ * split into bands of band_rows output rows -- the first output row it
+ * computes, the first and the number of output rows it adds (the last band
+ * is moved up to end at the job's last row), the input row of its buffer's
+ * first row and its input rows.  Returns the number of bands, -1 on an invalid argument. */
+IMFCS_API int imfcs_band_window(const imfcs_config *cfg, int band_rows, int band, int *out_row0, int *new_row0,
+                                int *new_rows, int *in_row0, int *in_rows);
+
 /* FCS diffusion law (dlfit, java:11007-11231, determineDiffusionLaw 8190-8250,
  * fitDiffLaw 8253-8295): for binnings 1..n_bin the whole path is run on the
  * device-resident stack; out[3*n_bin] = {Aeff [um^2], mean D [um^2/s],
