@@ -22,8 +22,12 @@ the ones it computes:
 * "PSF": the PSF calibration's rows (label, mean D, SD per binning) per PSF
   size, side by side.
 
-Sheets the engine has no data for (fit functions, residuals, MSD, dCCF,
-maps) are present and empty, so that readers that address sheets by name or
+* "Fit functions (ACF1)" / "Residuals (ACF1)" (or "(CCF)"): a fitted
+  pixel's model curve at the fit's lags and its residuals weighted as the
+  fit saw them, 0 for pixels without a fit (java:10383-10397, 10701-10710;
+  `model.fit_curves`), laid out as the ACF sheet.
+
+Sheets the engine has no data for (MSD, dCCF, maps) are present and empty, so that readers that address sheets by name or
 position find them.  Excel caps sheet names at 31 characters; the plugin's
 "Reconstruction Control Parameters" (33) is cut to 31.  Plain OOXML from the
 standard library (zipfile); numbers as numbers, NaN as an empty cell.
@@ -191,8 +195,27 @@ def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, dif
         for c in range(w * h):
             for i in range(ch):
                 wb.set(sheet, i + 1, c, float(data[c, i]))
-    # fit parameters
+    # fit functions and residuals of the fitted pixels
     fr = results.get("fitres")
+    acf = results.get("acf")
+    var = results.get("var")
+    if var is None and sd is not None:
+        var = np.asarray(sd, float) ** 2
+    if fr is not None and acf is not None and results.get("fitted") is not None and \
+            (var is not None if not cfg.gls else results.get("covmats") is not None):
+        from .model import fit_curves
+        fs = max(int(cfg.fitstart), 1)
+        fe = ch - 1 if cfg.fitend is None or cfg.fitend >= ch or cfg.fitend < fs else int(cfg.fitend)
+        fit, res = fit_curves(acf, fr, results["fitted"], cfg.cst, lagtime, var=var,
+                              covmats=results.get("covmats"), gls=bool(cfg.gls), fitstart=fs, fitend=fe)
+        tag = "CCF" if ccf else "ACF1"
+        for data, sheet in ((fit, f"Fit functions ({tag})"), (res, f"Residuals ({tag})")):
+            for c, lab in label.items():
+                wb.set(sheet, 0, c, lab)
+            for c in range(w * h):
+                for i in range(ch):
+                    wb.set(sheet, i + 1, c, float(data[c, i]))
+    # fit parameters
     if fr is not None:
         wb.set(fit_sheet, 0, 0, "Parameter")
         wb.set(fit_sheet, 1, 0, "fitted")

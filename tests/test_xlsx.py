@@ -93,3 +93,55 @@ def test_plan_results_roundtrip(tmp_path):
             if np.isfinite(res["acf"][c, i]):
                 assert s["ACF1"][(i + 1, c)] == res["acf"][c, i]
         assert s["Fit Parameters (ACF1)"][(2, c + 1)] == float(res["fitres"][c, 0])
+
+
+def test_fit_function_sheets(tmp_path):
+    """Fit functions and residuals: the model at the fitted parameters over
+    the fit range, (acf - fit) / sd there, 0 elsewhere and for pixels
+    without a fit (java:10383-10397)."""
+    from imaging_fcs_1_52_gb300 import model
+    cfg = engine.FCSConfig(width=5, height=4, frames=3000, background=100, fitstart=2, fitend=50)
+    rng = np.random.default_rng(1)
+    n, ch = cfg.npix, cfg.chanum
+    fitres = np.zeros((n, 11), np.float32)
+    fitres[:, 0] = rng.uniform(1, 3, n)
+    fitres[:, 1] = rng.uniform(0.5, 3, n) * 1e-12
+    lag, _ = engine.lag_tables(16, 8)
+    truth = model.fcs_model(fitres.astype(float), cfg.cst, lag * 1e-3)
+    res = {"acf": truth + rng.normal(0, 1e-3, (n, ch)), "var": np.full((n, ch), 4e-6), "fitres": fitres,
+           "chi2": np.ones(n, np.float32), "fitted": (np.arange(n) % 3 != 1).astype(np.int32)}
+    p = tmp_path / "f.xlsx"
+    xlsx.write_results(str(p), cfg, res)
+    _, s = read_xlsx(p)
+    fs, rs = s["Fit functions (ACF1)"], s["Residuals (ACF1)"]
+    assert fs[(0, 7)] == "(2, 1)" and rs[(0, 7)] == "(2, 1)"
+    for c in range(n):
+        for i in (1, 2, 30, 50, 51, 72):
+            if res["fitted"][c] and 2 <= i <= 50:
+                assert fs[(i + 1, c)] == pytest.approx(truth[c, i], rel=1e-12)
+                assert rs[(i + 1, c)] == pytest.approx((res["acf"][c, i] - truth[c, i]) / 2e-3, rel=1e-9)
+            else:
+                assert fs[(i + 1, c)] == 0 and rs[(i + 1, c)] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("gls", [False, True])
+def test_fit_curves_reproduce_gpu_chi2(gls):
+    """The workbook's residuals of a GPU fit give back the fit's reduced
+    chi^2 (java:10403-10406 OLS, 10712-10715 GLS): sum of squared weighted
+    residuals over the fit's degrees of freedom."""
+    from imaging_fcs_1_52_gb300 import model
+    from tests.synth import brownian_stack
+    st = brownian_stack(8, 6, 20000, seed=7, density=2.0, cps=3e4)
+    cfg = engine.FCSConfig(width=8, height=6, frames=20000, background=100, gls=gls)
+    out = engine.run_host(st, cfg)
+    lag, _ = engine.lag_tables(cfg.p, cfg.q)
+    fit, res = model.fit_curves(out["acf"], out["fitres"], out["fitted"], cfg.cst, lag * cfg.frametime,
+                                var=out["var"], covmats=out.get("covmats"), gls=gls, fitstart=1,
+                                fitend=cfg.chanum - 1)
+    k = 3
+    ok = out["fitted"].astype(bool)
+    assert ok.sum() >= cfg.npix // 2
+    dof = (cfg.chanum - k - 1) if gls else ((cfg.chanum - 1 - 1) - k - 1)
+    chi2 = (res[:, 1:] ** 2).sum(axis=1) / dof
+    np.testing.assert_allclose(chi2[ok], out["chi2"][ok], rtol=2e-3)
