@@ -250,6 +250,11 @@ extern "C" int imfcs_bands_execute(imfcs_bands *b, const uint16_t *host_stack, c
                                    void *stream)
 {
     if (!b || !host_stack || !host_out) { set_error("null argument"); return 1; }
+    // a background image set on the band plan would hold one band's rows
+    if (plan_job(b->pl).bg_trace) {
+        set_error("a per-pixel background image is not supported on bands");
+        return 1;
+    }
     const imfcs_config &c = b->cfg;
     const BandGeom &g = b->g;
     const cudaStream_t s = (cudaStream_t)stream;
