@@ -123,7 +123,7 @@ def test_bands_refuse_a_background_image():
     """A background image on the band plan would cover one band's rows only:
     execution is refused."""
     import ctypes as C
-    cfg = engine.FCSConfig(width=8, height=8, frames=2000)
+    cfg = engine.FCSConfig(width=8, height=8, frames=6000)
     bands = engine.Bands(cfg, band_rows=3)
     rows = engine.band_windows(cfg, 3)[0]["in_rows"]
     bg = np.full((rows, cfg.width), 100.0)
@@ -131,5 +131,5 @@ def test_bands_refuse_a_background_image():
     _lib.check(L.imfcs_plan_set_background_image(L.imfcs_bands_plan(bands._h), C.c_void_p(bg.ctypes.data)),
                "imfcs_plan_set_background_image")
     with pytest.raises(_lib.ImfcsError, match="background image"):
-        bands.execute_host(np.zeros((2000, 8, 8), np.uint16))
+        bands.execute_host(np.zeros((6000, 8, 8), np.uint16))
     bands.close()
