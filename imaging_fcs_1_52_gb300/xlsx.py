@@ -27,6 +27,12 @@ the ones it computes:
   fit saw them, 0 for pixels without a fit (java:10383-10397, 10701-10710;
   `model.fit_curves`), laid out as the ACF sheet.
 
+* "N&B": number and brightness of every pixel from the lag-1 monitor and
+  covariance of an autocorrelation (the plugin's GPU "G1" mode,
+  java:7828-7834): B = (cov - cov0) / mean, N = mean^2 / (cov - cov0), cov0
+  the background file's covariance image (0 without one); the "corrected"
+  rows, which that mode leaves unset, stay empty (java:4999-5017).
+
 Sheets the engine has no data for (MSD, dCCF, maps) are present and empty, so that readers that address sheets by name or
 position find them.  Excel caps sheet names at 31 characters; the plugin's
 "Reconstruction Control Parameters" (33) is cut to 31.  Plain OOXML from the
@@ -138,15 +144,27 @@ def _bleach_name(cfg) -> str:
             _lib.BLEACH_DOUBLE_EXP: "Double Exp", _lib.BLEACH_POLYNOMIAL: "Polynomial"}.get(cfg.bleach, "")
 
 
+def nb_maps(nb_mean, nb_cov, background_covariance=None):
+    """Number and brightness per pixel from the lag-1 mean and covariance
+    (java:7828-7834): B = (cov - cov0) / mean, N = mean^2 / (cov - cov0)."""
+    m = np.asarray(nb_mean, float)
+    c = np.asarray(nb_cov, float) - (0.0 if background_covariance is None else
+                                     np.asarray(background_covariance, float).reshape(m.shape))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return m * m / c, c / m
+
+
 def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, diffusion_law=None,
-                  psf=None) -> None:
+                  psf=None, nb_background_covariance=None) -> None:
     """Write a plan's results (engine.Plan.execute_host outputs) in the plugin's
     workbook layout.  cfg: the engine.FCSConfig; results: acf, sd or var,
     fitres, chi2, fitted, blocked_ok (any may be missing); lagtime, samp:
     per-channel lag time (s) and bin width (default: the lag tables of
     cfg); diffusion_law: dict with "table" (n_bin x 3: Aeff um^2, mean D
     um^2/s, var D) and optionally "line" (intercept, slope) and "fit_range";
-    psf: array [psf][3][n_bin] from imfcs_psf_calibration."""
+    psf: array [psf][3][n_bin] from imfcs_psf_calibration;
+    nb_background_covariance: the background file's covariance image
+    [out_h][out_w] for the N&B sheet (imfcs_background_stats)."""
     wb = Workbook()
     w, h = cfg.out_w, cfg.out_h
     # Panel Parameters: the plugin's first rows, values where a plan has them
@@ -236,6 +254,15 @@ def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, dif
                 wb.set(fit_sheet, len(PARAM_NAMES) + 3, c + 1, float(blocked[c]))
             if fitted is not None:
                 wb.set(fit_sheet, len(PARAM_NAMES) + 4, c + 1, float(fitted[c]))
+    # N&B of an autocorrelation
+    if not ccf and results.get("nb_mean") is not None and results.get("nb_cov") is not None:
+        num, bright = nb_maps(results["nb_mean"], results["nb_cov"], nb_background_covariance)
+        for r, nm in enumerate((" ", "Number", "Brightness", "Num (corrected)", "Epsilon (corrected)")):
+            wb.set("N&B", r, 0, nm)
+        for c, lab in label.items():
+            wb.set("N&B", 0, c + 2, lab)
+            wb.set("N&B", 1, c + 2, float(num[c]))
+            wb.set("N&B", 2, c + 2, float(bright[c]))
     # diffusion law
     if diffusion_law is not None:
         t = np.asarray(diffusion_law["table"], float)

@@ -145,3 +145,30 @@ def test_fit_curves_reproduce_gpu_chi2(gls):
     dof = (cfg.chanum - k - 1) if gls else ((cfg.chanum - 1 - 1) - k - 1)
     chi2 = (res[:, 1:] ** 2).sum(axis=1) / dof
     np.testing.assert_allclose(chi2[ok], out["chi2"][ok], rtol=2e-3)
+
+
+def test_nb_sheet(tmp_path):
+    """N&B sheet (java:4999-5017): number and brightness from the lag-1 mean
+    and covariance (java:7828-7834), minus the background covariance."""
+    cfg = engine.FCSConfig(width=4, height=3, frames=3000)
+    rng = np.random.default_rng(2)
+    n = cfg.npix
+    res = {"nb_mean": rng.uniform(5, 50, n), "nb_cov": rng.uniform(1, 20, n)}
+    cov0 = rng.uniform(0, 0.5, (cfg.out_h, cfg.out_w))
+    p = tmp_path / "nb.xlsx"
+    xlsx.write_results(str(p), cfg, res, nb_background_covariance=cov0)
+    _, s = read_xlsx(p)
+    nb = s["N&B"]
+    assert nb[(1, 0)] == "Number" and nb[(2, 0)] == "Brightness" and nb[(4, 0)] == "Epsilon (corrected)"
+    for c in range(n):
+        x, y = c % cfg.out_w, c // cfg.out_w
+        d = res["nb_cov"][c] - cov0[y, x]
+        assert nb[(0, c + 2)] == f"({x}, {y})"
+        assert nb[(1, c + 2)] == pytest.approx(res["nb_mean"][c] ** 2 / d, rel=1e-14)
+        assert nb[(2, c + 2)] == pytest.approx(d / res["nb_mean"][c], rel=1e-14)
+        assert (3, c + 2) not in nb
+    # a cross-correlation has no N&B
+    ccf = engine.FCSConfig(width=4, height=3, frames=3000, cfx=1)
+    xlsx.write_results(str(p), ccf, {"nb_mean": res["nb_mean"][:ccf.npix], "nb_cov": res["nb_cov"][:ccf.npix]})
+    _, s = read_xlsx(p)
+    assert not s["N&B"]
