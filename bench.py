@@ -282,6 +282,57 @@ def surrogate_block(plan, stack, steps):
     return blk
 
 
+# FP32 operations of one point in one LM iteration of lm_tirf_kernel (the
+# default one-component model, counted in its source, transcendentals as
+# one): the model value and Jacobian -- tirf_terms 37 (p0 and 1/p0 5, the
+# square-pixel lateral factor 11, its derivative chain 7, axial factor and
+# derivative 9, products 5), tirf_f 7 -- plus the normal equations of K = 3
+# free parameters, 2K + K(K+1) = 18.
+FIT_OPS_PER_POINT_ITERATION = 37 + 7 + 18
+MLP_FLOP_PER_SAMPLE = 2 * (128 * 256 + 256 * 256 + 256 * 4)   # forward GEMMs
+
+
+def compute_rooflines(L, cfg, fits_ms, iterations_total):
+    """Fit stage against the FP32 issue rate (measured by the library's FMA
+    probe; one FMA = one operation) and the surrogate's forward pass against
+    the measured bf16 tensor peak."""
+    import ctypes as C
+    import torch
+    from imaging_fcs_1_52_gb300 import _lib, surrogate
+    out = {}
+    rate = C.c_double()
+    _lib.check(L.imfcs_measure_fp32_fma_rate(C.byref(rate), None), "imfcs_measure_fp32_fma_rate")
+    peak_g = rate.value / 1e9
+    npts = (cfg.chanum - 1 if cfg.fitend is None else cfg.fitend) - cfg.fitstart + 1
+    ops = float(iterations_total) * npts * FIT_OPS_PER_POINT_ITERATION
+    ach = ops / (fits_ms * 1e-3) / 1e9
+    out["fit"] = {"kernel": "fit stage (ols_prepare, lm_tirf_kernel, fit_epilogue)", "bound": "fp32 issue",
+                  "unit": "G FP32 op/s", "achieved": ach, "peak": peak_g, "frac": ach / peak_g,
+                  "peak_kind": "measured (FMA probe)", "ops_per_point_iteration": FIT_OPS_PER_POINT_ITERATION,
+                  "points": npts, "iterations_total": int(iterations_total), "fits_ms": fits_ms}
+    if os.path.exists(surrogate.DEFAULT_WEIGHTS):
+        sur = surrogate.Surrogate.load()
+        n = cfg.npix
+        x = torch.randn((n, 128), device="cuda")
+        sur.predict(x)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(10):
+            e0.record()
+            sur.predict(x)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = statistics.median(ts)
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] \
+            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+        tf = MLP_FLOP_PER_SAMPLE * n / (ms * 1e-3) / 1e12
+        out["mlp"] = {"kernel": "surrogate predict (standardise, 3 bf16 mma.sync GEMMs with fused epilogues)",
+                      "bound": "tensor", "unit": "TFLOP/s", "achieved": tf, "peak": peak, "frac": tf / peak,
+                      "rows": n, "ms": ms, "flop_per_row": MLP_FLOP_PER_SAMPLE}
+    return out
+
+
 def bands_block(engine, cfg, host_np, whole_out, tile, steps):
     """Band-streamed host execution (imfcs_bands_*) of the same pinned stack
     under a device budget of a quarter of the one-band footprint, with the
@@ -500,6 +551,11 @@ def main():
             parity["bleach_rate_undetermined"] = int((~det).sum())
             parity["determined"] = parity_block(gpu_np, ref, cpu_n, det)
         fitted = int(out["fitted"].sum().item())
+        try:
+            rooflines = compute_rooflines(_lib.load(), cfg, stage_acc["fits"] / args.steps,
+                                          int(out["iterations"].sum().item()))
+        except Exception as e:   # reported, never fatal to the bench line
+            rooflines = {"error": str(e)}
         sur_blk = surrogate_block(plan, stack, args.steps)
         bands_blk = (bands_block(engine, cfg, host_np, outs_host, plan.corr_tile(), min(args.steps, 5))
                      if world == 1 else None)
@@ -529,6 +585,7 @@ def main():
                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": load_profile_traffic(),
                          "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": corr_avg},
+            "rooflines_other": rooflines,
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"{cpu_n} pixels x {T} frames of the same stack, FP64 C oracle, "
                                        f"{cpu_dt:.1f} s"},

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libimfcs_gb300.so")
 SOURCES = ["imfcs_stream.cu", "imfcs_corr2.cu", "imfcs_prep.cu", "imfcs_corr.cu", "imfcs_fit.cu", "imfcs_lm3.cu", "imfcs_lm5.cu", "imfcs_lm11.cu", "imfcs_lm_tirf.cu", "imfcs_gls.cu", "imfcs_capi.cu",
            "imfcs_ref_api.cu", "imfcs_sim.cu", "imfcs_noalloc.cu", "imfcs_mlp.cu", "imfcs_batch.cu", "imfcs_ingest.cu",
-           "imfcs_band.cu"]
+           "imfcs_band.cu", "imfcs_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "-I", INCLUDE, "-I", CSRC]

@@ -382,6 +382,12 @@ IMFCS_API int imfcs_bands_geometry(const imfcs_bands *bands, int *band_rows, int
 IMFCS_API imfcs_plan *imfcs_bands_plan(imfcs_bands *bands);
 IMFCS_API int imfcs_bands_execute(imfcs_bands *bands, const uint16_t *host_stack, const imfcs_outputs *host_out,
                                   void *stream);
+/* FP32 issue-rate probe (no counterpart in the reference): FMA
+ * instructions per second the device sustains over independent chains on
+ * every SM (best of five timed launches); the denominator of the fit
+ * stage's roofline. */
+IMFCS_API int imfcs_measure_fp32_fma_rate(double *fma_per_s, void *stream);
+
 /* Band split without a device (host arithmetic only): band `band` of a job
  * split into bands of band_rows output rows -- the first output row it
  * computes, the first and the number of output rows it adds (the last band

@@ -118,3 +118,26 @@ def test_config_defaults_follow_the_plugin():
     assert cfg.init[0] == 1.0 and cfg.init[1] == 1e-12 and cfg.free_mask[:5] == (1, 1, 0, 0, 1)
     c = cfg.to_c()
     assert c.fitend == 72 and c.max_iter == 2000
+
+
+@pytest.mark.gpu
+def test_fp32_fma_probe_rate_is_plausible():
+    """The FP32 issue-rate probe (the fit roofline's denominator) reports a
+    rate between a few T and 100 T FMA/s on one GPU."""
+    L = _lib.load()
+    r = C.c_double()
+    _lib.check(L.imfcs_measure_fp32_fma_rate(C.byref(r), None), "imfcs_measure_fp32_fma_rate")
+    assert 5e12 < r.value < 1e14
+
+
+def test_fp32_fma_probe_without_device():
+    if torch_cuda_available():
+        pytest.skip("a device is present")
+    L = _lib.load()
+    r = C.c_double()
+    assert L.imfcs_measure_fp32_fma_rate(C.byref(r), None) != 0 and _lib.last_error()
+
+
+def torch_cuda_available() -> bool:
+    import torch
+    return torch.cuda.is_available()
