@@ -40,7 +40,7 @@ EXPORTS = [
     "imfcs_batch_kernel_launches",
     "imfcs_tiff_open", "imfcs_tiff_read", "imfcs_tiff_read_device", "imfcs_tiff_close", "imfcs_background_stats",
     "imfcs_bands_create", "imfcs_bands_destroy", "imfcs_bands_geometry", "imfcs_bands_plan", "imfcs_bands_execute",
-    "imfcs_band_window", "imfcs_measure_fp32_fma_rate",
+    "imfcs_band_window", "imfcs_measure_fp32_fma_rate", "imfcs_bands_set_background_image",
 ]
 
 
@@ -173,6 +173,7 @@ def _declare(L: C.CDLL) -> None:
     L.imfcs_bands_plan.argtypes = [vp]
     L.imfcs_bands_execute.argtypes = [vp, vp, C.POINTER(Outputs), vp]
     L.imfcs_measure_fp32_fma_rate.argtypes = [dp, vp]
+    L.imfcs_bands_set_background_image.argtypes = [vp, vp]
     L.imfcs_band_window.argtypes = [C.POINTER(Config), C.c_int, C.c_int, ip, ip, ip, ip, ip]
 
 

@@ -30,7 +30,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
+#include <vector>
 
 #include "imfcs_gb300.h"
 #include "imfcs_host.h"
@@ -114,6 +116,7 @@ struct imfcs_bands {
     size_t bytes = 0;                  // device bytes held (plan, buffers, outputs)
     cudaStream_t copy = nullptr;
     cudaEvent_t copied[2] = {}, consumed[2] = {};
+    std::vector<double> bg;            // per-pixel background image [height][width] (empty: scalar)
     ~imfcs_bands()
     {
         if (copy) cudaStreamSynchronize(copy);
@@ -237,6 +240,23 @@ extern "C" int imfcs_bands_geometry(const imfcs_bands *b, int *band_rows, int *n
 
 extern "C" imfcs_plan *imfcs_bands_plan(imfcs_bands *b) { return b ? b->pl : nullptr; }
 
+extern "C" int imfcs_bands_set_background_image(imfcs_bands *b, const double *host_bg)
+{
+    if (!b) { set_error("null bands"); return 1; }
+    if (!host_bg) {
+        b->bg.clear();
+        return imfcs_plan_set_background_image(b->pl, nullptr);
+    }
+    const size_t n = (size_t)b->cfg.width * b->cfg.height;
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(host_bg[i]) || host_bg[i] < -2e9 || host_bg[i] > 2e9) {
+            set_error("background image holds an invalid value");
+            return 1;
+        }
+    b->bg.assign(host_bg, host_bg + n);
+    return 0;
+}
+
 template <class T>
 static cudaError_t band_d2h(T *host, const T *dev, size_t host_px, size_t dev_px, size_t n_px, size_t per_px,
                             cudaStream_t s)
@@ -250,9 +270,10 @@ extern "C" int imfcs_bands_execute(imfcs_bands *b, const uint16_t *host_stack, c
                                    void *stream)
 {
     if (!b || !host_stack || !host_out) { set_error("null argument"); return 1; }
-    // a background image set on the band plan would hold one band's rows
-    if (plan_job(b->pl).bg_trace) {
-        set_error("a per-pixel background image is not supported on bands");
+    // a background image set on the band plan directly would hold one
+    // band's rows; imfcs_bands_set_background_image sets each band's
+    if (b->bg.empty() && plan_job(b->pl).bg_trace) {
+        set_error("set a per-pixel background image of bands with imfcs_bands_set_background_image");
         return 1;
     }
     const imfcs_config &c = b->cfg;
@@ -303,6 +324,12 @@ extern "C" int imfcs_bands_execute(imfcs_bands *b, const uint16_t *host_stack, c
         // the next band's copy is queued before this band's results are read
         // back, so that it overlaps this band's execution
         if (k + 1 < g.bands && enqueue_copy(k + 1)) return 1;
+        if (!b->bg.empty()) {
+            // the band's rows of the background image; the previous band's
+            // kernels read the plan's background sums until they finish
+            CK(cudaStreamSynchronize(s));
+            if (imfcs_plan_set_background_image(b->pl, b->bg.data() + (size_t)w.in_row0 * W)) return 1;
+        }
         CK(cudaStreamWaitEvent(s, b->copied[i], 0));
         if (imfcs_plan_execute(b->pl, b->buf[i], &b->dout, s)) return 1;
         CK(cudaEventRecord(b->consumed[i], s));

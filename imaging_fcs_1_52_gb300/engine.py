@@ -478,6 +478,18 @@ class Bands:
         check(self._L.imfcs_plan_set_corr_tile(self._L.imfcs_bands_plan(self._h), int(cta), int(seg_extra), int(t)),
               "imfcs_plan_set_corr_tile")
 
+    def set_background_image(self, bg):
+        """Per-pixel background [height][width] of the whole input frame
+        (imfcs_bands_set_background_image); None = the scalar one."""
+        if bg is None:
+            check(self._L.imfcs_bands_set_background_image(self._h, None), "imfcs_bands_set_background_image")
+            return
+        a = np.ascontiguousarray(bg, np.float64)
+        if a.shape != (self.cfg.height, self.cfg.width):
+            raise ValueError(f"background image must be {self.cfg.height} x {self.cfg.width}")
+        check(self._L.imfcs_bands_set_background_image(self._h, C.c_void_p(a.ctypes.data)),
+              "imfcs_bands_set_background_image")
+
     def execute_host(self, stack: np.ndarray, outputs: dict | None = None, stream=None) -> dict:
         """Host stack [frames][height][width] in, host results out."""
         stack = np.ascontiguousarray(stack, dtype=np.uint16)

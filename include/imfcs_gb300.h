@@ -370,16 +370,20 @@ IMFCS_API int imfcs_plan_synchronize(imfcs_plan *plan, void *stream);
  * while the previous band computes; results equal imfcs_plan_execute_host's
  * on the whole stack, since output pixels are independent.
  * imfcs_bands_execute returns after the results are in host_out (pinned
- * host buffers let copies and computation overlap).  A per-pixel background
- * image is not supported on bands (scalar background only). */
+ * host buffers let copies and computation overlap). */
 typedef struct imfcs_bands imfcs_bands;
 IMFCS_API int imfcs_bands_create(const imfcs_config *cfg, int band_rows, size_t max_device_bytes,
                                  imfcs_bands **bands);
 IMFCS_API int imfcs_bands_destroy(imfcs_bands *bands);
 /* Output rows per band, number of bands, device bytes held. */
 IMFCS_API int imfcs_bands_geometry(const imfcs_bands *bands, int *band_rows, int *n_bands, size_t *device_bytes);
-/* The plan that runs every band (for its tile, timing and surrogate settings). */
+/* The plan that runs every band (for its tile, timing and surrogate settings;
+ * a background image goes through imfcs_bands_set_background_image). */
 IMFCS_API imfcs_plan *imfcs_bands_plan(imfcs_bands *bands);
+/* Per-pixel background image [height][width] of the whole input frame (as
+ * imfcs_plan_set_background_image; NULL: the scalar background); each band
+ * takes its rows (copied: the caller's array may be freed). */
+IMFCS_API int imfcs_bands_set_background_image(imfcs_bands *bands, const double *host_bg);
 IMFCS_API int imfcs_bands_execute(imfcs_bands *bands, const uint16_t *host_stack, const imfcs_outputs *host_out,
                                   void *stream);
 /* FP32 issue-rate probe (no counterpart in the reference): FMA

@@ -133,3 +133,25 @@ def test_bands_refuse_a_background_image():
     with pytest.raises(_lib.ImfcsError, match="background image"):
         bands.execute_host(np.zeros((6000, 8, 8), np.uint16))
     bands.close()
+
+
+@pytest.mark.gpu
+def test_bands_with_a_background_image_match_whole_stack():
+    """A per-pixel background image on bands (each band takes its rows)
+    gives the whole-stack results with the same image."""
+    from tests.synth import brownian_stack
+    geo = dict(width=12, height=21, binx=2, biny=2, pixbinx=1, pixbiny=1, cfx=1, cfy=-1, map_y0=1, out_h=18)
+    st = brownian_stack(12, 21, 6000, seed=13, density=2.0, cps=3e4)
+    cfg = engine.FCSConfig(frames=6000, background=100, **geo)
+    bg = np.random.default_rng(3).uniform(95.0, 105.0, (21, 12))
+    plan = engine.Plan(cfg)
+    plan.set_background_image(bg)
+    whole = plan.execute_host(st)
+    plan.close()
+    bands = engine.Bands(cfg, band_rows=5)
+    bands.set_background_image(bg)
+    _compare(whole, bands.execute_host(st), engine.output_names(cfg))
+    # back to the scalar background
+    bands.set_background_image(None)
+    _compare(engine.run_host(st, cfg), bands.execute_host(st), engine.output_names(cfg))
+    bands.close()
