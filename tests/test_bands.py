@@ -155,3 +155,69 @@ def test_bands_with_a_background_image_match_whole_stack():
     bands.set_background_image(None)
     _compare(engine.run_host(st, cfg), bands.execute_host(st), engine.output_names(cfg))
     bands.close()
+
+
+@pytest.mark.parametrize("geo,band_rows", [
+    (dict(width=9, height=14, cfy=2), 4),
+    (dict(width=9, height=14, cfx=1, cfy=-1, map_y0=1, out_h=13), 3),
+    (dict(width=10, height=17, binx=2, biny=2, pixbinx=1, pixbiny=1, cfy=-3, map_y0=3, out_h=12), 5),
+    (dict(width=14, height=25, binx=3, biny=3, cfy=-2, map_y0=1, out_h=6), 4),
+])
+def test_band_decomposition_preserves_every_pixel_on_the_oracle(geo, band_rows):
+    """The band split on the CPU, with the oracle as each band's engine:
+    every band's sub-stack (its input rows, frames first..first+num-1) under
+    the band geometry (map_y0 = the halo's pixel steps, out_h = band rows)
+    gives the whole stack's per-pixel results."""
+    import oracle
+    from tests.synth import brownian_stack
+    cfg = engine.FCSConfig(frames=3000, first=200, background=100, **geo)
+    st = brownian_stack(cfg.width, cfg.height, 3000, seed=21, density=2.0, cps=3e4)
+    kw = dict(out_w=cfg.out_w, map_x0=cfg.map_x0, binx=cfg.binx, biny=cfg.biny, pixbinx=cfg.pixbinx,
+              pixbiny=cfg.pixbiny, cfx=cfg.cfx, cfy=cfg.cfy, background=100, p=16, q=7, do_fit=False)
+    whole = oracle.run(st, out_h=cfg.out_h, map_y0=cfg.map_y0, first=cfg.first, num=cfg.num, **kw)
+    got = {k: np.full_like(whole[k], -7) for k in ("acf", "var", "blocked_ind", "blocked_ok")}
+    for w in engine.band_windows(cfg, band_rows):
+        rows = min(band_rows, cfg.out_h)
+        m = cfg.map_y0 + w["out_row0"] - w["in_row0"] // cfg.pixbiny
+        assert w["in_row0"] % cfg.pixbiny == 0 and m >= 0
+        sub = st[cfg.first:cfg.first + cfg.num, w["in_row0"]:w["in_row0"] + w["in_rows"]]
+        band = oracle.run(sub, out_h=rows, map_y0=m, **kw)
+        skip = w["new_row0"] - w["out_row0"]
+        for k in got:
+            got[k][w["new_row0"] * cfg.out_w:(w["new_row0"] + w["new_rows"]) * cfg.out_w] = \
+                band[k][skip * cfg.out_w:(skip + w["new_rows"]) * cfg.out_w]
+    for k in got:
+        np.testing.assert_array_equal(got[k], whole[k], err_msg=k)
+
+
+def test_band_split_random_geometries():
+    """imfcs_band_window over 300 random valid geometries: rows added once
+    each, windows inside the band buffer, buffer inside the image."""
+    rng = np.random.default_rng(8)
+    checked = 0
+    while checked < 300:
+        b = int(rng.integers(1, 5))
+        over = bool(rng.integers(0, 2))
+        step = 1 if over else b
+        cfy = int(rng.integers(-4, 5))
+        h = int(rng.integers(b + abs(cfy) + 1, 40))
+        y0min = -(-max(0, -cfy) // step)                 # first map row whose window stays in the image
+        rows_max = (h - 1 - max(0, cfy) - (b - 1)) // step + 1 - y0min
+        if rows_max < 1:
+            continue
+        map_y0 = int(rng.integers(y0min, y0min + rows_max))
+        out_h = int(rng.integers(1, rows_max - (map_y0 - y0min) + 1))
+        cfg = engine.FCSConfig(width=6, height=h, frames=100, binx=b, biny=b, pixbinx=step, pixbiny=step,
+                               cfy=cfy, map_y0=map_y0, out_h=out_h)
+        band_rows = int(rng.integers(1, out_h + 2))
+        wins = engine.band_windows(cfg, band_rows)
+        rows = min(band_rows, out_h)
+        added = []
+        for w in wins:
+            added += range(w["new_row0"], w["new_row0"] + w["new_rows"])
+            assert 0 <= w["in_row0"] and w["in_row0"] + w["in_rows"] <= h
+            for oy in range(w["out_row0"], w["out_row0"] + rows):
+                lo, hi = _windows_rows(cfg, oy)
+                assert w["in_row0"] <= lo and hi < w["in_row0"] + w["in_rows"]
+        assert added == list(range(out_h))
+        checked += 1
