@@ -149,8 +149,8 @@ class GpufitImFCS:
 
     @staticmethod
     def calcDataBleachCorrection(pixels: np.ndarray, outdata: np.ndarray, params: ACFParameters) -> None:
-        GpufitImFCS._call("imfcs_calc_data_bleach_correction", _f32(pixels), _f32(outdata, out=True),
-                          C.byref(params))
+        src = _f32_in(pixels)
+        GpufitImFCS._call("imfcs_calc_data_bleach_correction", _p(src), _f32_out(outdata), C.byref(params))
 
     @staticmethod
     def isBinningMemorySufficient(params: ACFParameters) -> bool:
@@ -158,7 +158,8 @@ class GpufitImFCS:
 
     @staticmethod
     def calcBinning(indata: np.ndarray, outdata: np.ndarray, params: ACFParameters) -> None:
-        GpufitImFCS._call("imfcs_calc_binning", _f32(indata), _f32(outdata, out=True), C.byref(params))
+        src = _f32_in(indata)
+        GpufitImFCS._call("imfcs_calc_binning", _p(src), _f32_out(outdata), C.byref(params))
 
     @staticmethod
     def isACFmemorySufficient(params: ACFParameters) -> bool:
@@ -173,7 +174,8 @@ class GpufitImFCS:
             assert a.dtype == np.float64 and a.flags.c_contiguous
             return C.c_void_p(a.ctypes.data)
         assert lag.dtype == np.int32
-        GpufitImFCS._call("imfcs_calc_acf", _f32(pixels), dptr(pixels1), dptr(blockvararray), dptr(NBmeanGPU),
+        src = _f32_in(pixels)
+        GpufitImFCS._call("imfcs_calc_acf", _p(src), dptr(pixels1), dptr(blockvararray), dptr(NBmeanGPU),
                           dptr(NBcovarianceGPU), dptr(blocked1D), dptr(bleachcorr_params), dptr(samp),
                           C.c_void_p(lag.ctypes.data), C.byref(params))
 
@@ -183,15 +185,15 @@ class GpufitImFCS:
             raise RuntimeError(GpufitImFCS.getLastError())
 
 
-def _f32(a, out=False):
-    if out:
-        assert a.dtype == np.float32 and a.flags.c_contiguous, "output arrays must be contiguous float32"
-        return C.c_void_p(a.ctypes.data)
-    a = np.ascontiguousarray(a, np.float32)
-    _keep.append(a)
-    if len(_keep) > 8:
-        del _keep[:-8]
+def _f32_in(a) -> np.ndarray:
+    """A contiguous float32 view or copy of an input array; the caller keeps
+    it alive across the library call."""
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _f32_out(a) -> C.c_void_p:
+    """Output arrays are filled in place, so they must already be contiguous
+    float32 (the Java float[] the native writes into)."""
+    if a.dtype != np.float32 or not a.flags.c_contiguous:
+        raise ValueError("output arrays must be contiguous float32")
     return C.c_void_p(a.ctypes.data)
-
-
-_keep: list = []
