@@ -317,39 +317,49 @@ extern "C" int imfcs_bands_execute(imfcs_bands *b, const uint16_t *host_stack, c
         CK(cudaEventRecord(b->copied[i], b->copy));
         return 0;
     };
-    if (enqueue_copy(0)) return 1;
-    for (int k = 0; k < g.bands; k++) {
-        const int i = k & 1;
-        const BandWin w = band_win(c, g, k);
-        // the next band's copy is queued before this band's results are read
-        // back, so that it overlaps this band's execution
-        if (k + 1 < g.bands && enqueue_copy(k + 1)) return 1;
-        if (!b->bg.empty()) {
-            // the band's rows of the background image; the previous band's
-            // kernels read the plan's background sums until they finish
-            CK(cudaStreamSynchronize(s));
-            if (imfcs_plan_set_background_image(b->pl, b->bg.data() + (size_t)w.in_row0 * W)) return 1;
+    auto enqueue_all = [&]() -> int {
+        if (enqueue_copy(0)) return 1;
+        for (int k = 0; k < g.bands; k++) {
+            const int i = k & 1;
+            const BandWin w = band_win(c, g, k);
+            // the next band's copy is queued before this band's results are read
+            // back, so that it overlaps this band's execution
+            if (k + 1 < g.bands && enqueue_copy(k + 1)) return 1;
+            if (!b->bg.empty()) {
+                // the band's rows of the background image; the previous band's
+                // kernels read the plan's background sums until they finish
+                CK(cudaStreamSynchronize(s));
+                if (imfcs_plan_set_background_image(b->pl, b->bg.data() + (size_t)w.in_row0 * W)) return 1;
+            }
+            CK(cudaStreamWaitEvent(s, b->copied[i], 0));
+            if (imfcs_plan_execute(b->pl, b->buf[i], &b->dout, s)) return 1;
+            CK(cudaEventRecord(b->consumed[i], s));
+            const imfcs_outputs &d = b->dout;
+            const size_t hp = (size_t)w.new_row0 * c.out_w;                  // first new pixel, whole job
+            const size_t dp = (size_t)(w.new_row0 - w.out_row0) * c.out_w;   // same pixel, in the band
+            const size_t np = (size_t)w.new_rows * c.out_w;
+            CK(band_d2h(host_out->acf, d.acf, hp, dp, np, ch, s));
+            CK(band_d2h(host_out->var, d.var, hp, dp, np, ch, s));
+            CK(band_d2h(host_out->sd, d.sd, hp, dp, np, ch, s));
+            CK(band_d2h(host_out->blocked_ind, d.blocked_ind, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->blocked_ok, d.blocked_ok, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->nb_mean, d.nb_mean, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->nb_cov, d.nb_cov, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->fitres, d.fitres, hp, dp, np, IMFCS_NPARAM, s));
+            CK(band_d2h(host_out->chi2, d.chi2, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->fitted, d.fitted, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->iterations, d.iterations, hp, dp, np, 1, s));
+            CK(band_d2h(host_out->bayes_prob, d.bayes_prob, hp, dp, np, 2, s));
+            CK(band_d2h(host_out->covmats, d.covmats, hp, dp, np, (ch - 1) * (ch - 1), s));
         }
-        CK(cudaStreamWaitEvent(s, b->copied[i], 0));
-        if (imfcs_plan_execute(b->pl, b->buf[i], &b->dout, s)) return 1;
-        CK(cudaEventRecord(b->consumed[i], s));
-        const imfcs_outputs &d = b->dout;
-        const size_t hp = (size_t)w.new_row0 * c.out_w;                  // first new pixel, whole job
-        const size_t dp = (size_t)(w.new_row0 - w.out_row0) * c.out_w;   // same pixel, in the band
-        const size_t np = (size_t)w.new_rows * c.out_w;
-        CK(band_d2h(host_out->acf, d.acf, hp, dp, np, ch, s));
-        CK(band_d2h(host_out->var, d.var, hp, dp, np, ch, s));
-        CK(band_d2h(host_out->sd, d.sd, hp, dp, np, ch, s));
-        CK(band_d2h(host_out->blocked_ind, d.blocked_ind, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->blocked_ok, d.blocked_ok, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->nb_mean, d.nb_mean, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->nb_cov, d.nb_cov, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->fitres, d.fitres, hp, dp, np, IMFCS_NPARAM, s));
-        CK(band_d2h(host_out->chi2, d.chi2, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->fitted, d.fitted, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->iterations, d.iterations, hp, dp, np, 1, s));
-        CK(band_d2h(host_out->bayes_prob, d.bayes_prob, hp, dp, np, 2, s));
-        CK(band_d2h(host_out->covmats, d.covmats, hp, dp, np, (ch - 1) * (ch - 1), s));
+        return 0;
+    };
+    if (enqueue_all()) {
+        // copies already queued still read the caller's stack and write its
+        // outputs: let them finish before the caller can free either
+        cudaStreamSynchronize(b->copy);
+        cudaStreamSynchronize(s);
+        return 1;
     }
     return imfcs_plan_synchronize(b->pl, stream);
 }
