@@ -40,6 +40,7 @@ standard library (zipfile); numbers as numbers, NaN as an empty cell.
 """
 from __future__ import annotations
 
+import functools
 import math
 import zipfile
 from xml.sax.saxutils import escape
@@ -59,6 +60,7 @@ SHEETS = [
 PARAM_NAMES = ["N", "D", "vx", "vy", "G", "F2", "D2", "F3", "D3", "Ftrip", "Ttrip"]
 
 
+@functools.lru_cache(maxsize=None)
 def _col(c: int) -> str:
     s = ""
     c += 1
@@ -82,12 +84,29 @@ def _cell(r: int, c: int, v) -> str:
     return f'<c r="{ref}"><v>{repr(x)}</v></c>'
 
 
-def _sheet_xml(rows: dict) -> str:
+def _block_row(r: int, c0: int, values) -> str:
+    """One row of a dense numeric block: cells c0, c0+1, ... (non-finite
+    values are left empty)."""
+    row = str(r + 1)
+    return "".join(f'<c r="{_col(c0 + j)}{row}"><v>{x!r}</v></c>'
+                   for j, x in enumerate(values) if math.isfinite(x))
+
+
+def _sheet_xml(rows: dict, blocks: list) -> str:
+    """rows: {row: {col: value}}; blocks: (r0, c0, 2-D float array) placed
+    with its element [i][j] at row r0 + i, column c0 + j.  Cells of a row
+    are written in column order."""
     out = ['<?xml version="1.0" encoding="UTF-8" standalone="yes"?>',
            '<worksheet xmlns="http://schemas.openxmlformats.org/spreadsheetml/2006/main"><sheetData>']
-    for r in sorted(rows):
-        cells = "".join(_cell(r, c, v) for c, v in sorted(rows[r].items()))
-        out.append(f'<row r="{r + 1}">{cells}</row>')
+    by_row: dict = {}
+    for r0, c0, a in blocks:
+        for i in range(a.shape[0]):
+            by_row.setdefault(r0 + i, []).append((c0, a[i]))
+    for r in sorted(set(rows) | set(by_row)):
+        segs = [(c, _cell(r, c, v)) for c, v in rows.get(r, {}).items()]
+        segs += [(c0, _block_row(r, c0, vals.tolist())) for c0, vals in by_row.get(r, [])]
+        segs.sort(key=lambda t: t[0])
+        out.append(f'<row r="{r + 1}">{"".join(t[1] for t in segs)}</row>')
     out.append("</sheetData></worksheet>")
     return "".join(out)
 
@@ -97,9 +116,14 @@ class Workbook:
 
     def __init__(self):
         self.cells = {name: {} for name in SHEETS}
+        self.blocks = {name: [] for name in SHEETS}
 
     def set(self, sheet: str, r: int, c: int, v):
         self.cells[sheet].setdefault(r, {})[c] = v
+
+    def set_block(self, sheet: str, r0: int, c0: int, values):
+        """Numbers values[i][j] at row r0 + i, column c0 + j (NaN: empty)."""
+        self.blocks[sheet].append((r0, c0, np.asarray(values, np.float64)))
 
     def save(self, path: str):
         ns = "http://schemas.openxmlformats.org/spreadsheetml/2006/main"
@@ -129,13 +153,13 @@ class Workbook:
         wrels += [f'<Relationship Id="rId{i + 1}" Type="{rel}/worksheet" Target="worksheets/sheet{i + 1}.xml"/>'
                   for i in range(n)]
         wrels.append("</Relationships>")
-        with zipfile.ZipFile(path, "w", zipfile.ZIP_DEFLATED) as z:
+        with zipfile.ZipFile(path, "w", zipfile.ZIP_DEFLATED, compresslevel=1) as z:
             z.writestr("[Content_Types].xml", "".join(ct))
             z.writestr("_rels/.rels", rels)
             z.writestr("xl/workbook.xml", "".join(wb))
             z.writestr("xl/_rels/workbook.xml.rels", "".join(wrels))
             for i, name in enumerate(SHEETS):
-                z.writestr(f"xl/worksheets/sheet{i + 1}.xml", _sheet_xml(self.cells[name]))
+                z.writestr(f"xl/worksheets/sheet{i + 1}.xml", _sheet_xml(self.cells[name], self.blocks[name]))
 
 
 def _bleach_name(cfg) -> str:
@@ -210,9 +234,7 @@ def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, dif
             continue
         for c, lab in label.items():
             wb.set(sheet, 0, c, lab)
-        for c in range(w * h):
-            for i in range(ch):
-                wb.set(sheet, i + 1, c, float(data[c, i]))
+        wb.set_block(sheet, 1, 0, np.asarray(data, float)[:w * h, :ch].T)
     # fit functions and residuals of the fitted pixels
     fr = results.get("fitres")
     acf = results.get("acf")
@@ -230,9 +252,7 @@ def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, dif
         for data, sheet in ((fit, f"Fit functions ({tag})"), (res, f"Residuals ({tag})")):
             for c, lab in label.items():
                 wb.set(sheet, 0, c, lab)
-            for c in range(w * h):
-                for i in range(ch):
-                    wb.set(sheet, i + 1, c, float(data[c, i]))
+            wb.set_block(sheet, 1, 0, data[:w * h, :ch].T)
     # fit parameters
     if fr is not None:
         wb.set(fit_sheet, 0, 0, "Parameter")
@@ -243,17 +263,14 @@ def write_results(path: str, cfg, results: dict, *, lagtime=None, samp=None, dif
         fitted = results.get("fitted")
         chi2 = results.get("chi2")
         blocked = results.get("blocked_ok")
+        npx = w * h
         for c, lab in label.items():
             wb.set(fit_sheet, 0, c + 1, lab)
             wb.set(fit_sheet, 1, c + 1, bool(fitted[c]) if fitted is not None else None)
-            for i in range(len(PARAM_NAMES)):
-                wb.set(fit_sheet, i + 2, c + 1, float(fr[c, i]))
-            if chi2 is not None:
-                wb.set(fit_sheet, len(PARAM_NAMES) + 2, c + 1, float(chi2[c]))
-            if blocked is not None:
-                wb.set(fit_sheet, len(PARAM_NAMES) + 3, c + 1, float(blocked[c]))
-            if fitted is not None:
-                wb.set(fit_sheet, len(PARAM_NAMES) + 4, c + 1, float(fitted[c]))
+        wb.set_block(fit_sheet, 2, 1, np.asarray(fr, float)[:npx, :len(PARAM_NAMES)].T)
+        for q, extra in enumerate((chi2, blocked, fitted)):
+            if extra is not None:
+                wb.set_block(fit_sheet, len(PARAM_NAMES) + 2 + q, 1, np.asarray(extra, float)[None, :npx])
     # N&B of an autocorrelation
     if not ccf and results.get("nb_mean") is not None and results.get("nb_cov") is not None:
         num, bright = nb_maps(results["nb_mean"], results["nb_cov"], nb_background_covariance)
